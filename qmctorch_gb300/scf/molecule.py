@@ -1,0 +1,316 @@
+"""Molecule and basis namespace: the input side of the VMC hot path.
+
+The AO layer of QMCTorch consumes a ``mol.basis`` namespace produced by its
+SCF calculator (``qmctorch/scf/calculator/pyscf.py:104-252``). pyscf is not
+available on the machines this package targets, so :class:`Molecule` builds
+the same namespace from the built-in basis tables (``basis_tables.py``) with
+the same entry layout:
+
+* one *entry* per (shell, general contraction, cartesian component,
+  primitive), in pyscf shell order (``pyscf.py:146-203``);
+* general-contraction column ``ictr`` divided by ``ictr + 1``
+  (``pyscf.py:172``);
+* cartesian component order ``xx, xy, xz, yy, yz, zz`` for d shells
+  (``pyscf.py:120-122``);
+* ``nshells`` = number of entries per atom, ``index_ctr`` = AO index of each
+  entry, ``nao_per_atom``, ``nctr_per_ao`` (``pyscf.py:206-223``);
+* ``mos`` column-normalised (``calculator_base.py:36-46``).
+
+Molecular orbitals come from an extended-Hueckel guess (Wolfsberg-Helmholz,
+K = 1.75) on the overlap matrix of the AOs exactly as the AO layer evaluates
+them; there is no Hartree-Fock solver here. ``nmo`` keeps the reference's
+count of spherical MOs (a d shell contributes 5), so the lowest ``nmo``
+Hueckel orbitals are kept.
+"""
+from __future__ import annotations
+
+import itertools
+import math
+from types import SimpleNamespace
+
+import numpy as np
+
+from .basis_tables import ATOMIC_NUMBER, BASIS_TABLES, HUCKEL_VSIE
+
+ANGS2BOHR = 1.8897259886  # qmctorch/utils/constants.py:1
+
+_KX = {0: [0], 1: [1, 0, 0], 2: [2, 1, 1, 0, 0, 0]}
+_KY = {0: [0], 1: [0, 1, 0], 2: [0, 1, 0, 2, 1, 0]}
+_KZ = {0: [0], 1: [0, 0, 1], 2: [0, 0, 1, 0, 1, 2]}
+_MV = {0: [0], 1: [-1, 0, 1], 2: [-2, -1, 0, 1, 2]}
+_DFACT = {-1: 1, 0: 1, 1: 1, 2: 2, 3: 3, 5: 15}
+
+
+def norm_gaussian_cartesian(kx, ky, kz, alpha):
+    """Per-entry norm of a cartesian GTO, as the AO layer computes it
+    (``qmctorch/wavefunction/orbitals/norm_orbital.py:136-161``):
+    (2a/pi)^(3/4) * prod_i (4a)^(k_i/2) / sqrt((2k_i-1)!!)."""
+    kx = np.asarray(kx)
+    ky = np.asarray(ky)
+    kz = np.asarray(kz)
+    alpha = np.asarray(alpha, dtype=np.float64)
+    pref = (2.0 * alpha / np.pi) ** 0.75
+    out = pref
+    for k in (kx, ky, kz):
+        df = np.array([_DFACT[int(2 * v - 1)] for v in k], dtype=np.float64)
+        out = out * (4.0 * alpha) ** (k / 2.0) / np.sqrt(df)
+    return out
+
+
+def build_basis_namespace(atoms, atom_coords, basis_name):
+    """Lay out the basis entries the way ``CalculatorPySCF.get_basis_data``
+    does (``qmctorch/scf/calculator/pyscf.py:104-252``)."""
+    table = BASIS_TABLES[basis_name.lower()]
+    natm = len(atoms)
+    nshells = [0] * natm
+    bas_coeff, bas_exp, index_ctr = [], [], []
+    bas_l, bas_m, bas_n, bas_kx, bas_ky, bas_kz = [], [], [], [], [], []
+    shell_info = []  # (atom, l, first AO, ncomp, role) for the Hueckel guess
+    iao = 0
+    for iat, sym in enumerate(atoms):
+        seen_s = 0
+        for lval, exps, coeffs in table[sym]:
+            coeffs = np.asarray(coeffs, dtype=np.float64)
+            exps = np.asarray(exps, dtype=np.float64)
+            nprim, nctr = coeffs.shape
+            ncart = len(_KX[lval])
+            for ictr in range(nctr):
+                cc = coeffs[:, ictr] / (ictr + 1)
+                bas_coeff += cc.tolist() * ncart
+                bas_exp += exps.tolist() * ncart
+                bas_l += [lval] * nprim * ncart
+                bas_n += [lval + 1] * nprim * ncart
+                nshells[iat] += nprim * ncart
+                if lval == 0:
+                    role = 0 if (seen_s == 0 and ATOMIC_NUMBER[sym] > 2) else 1
+                    seen_s += 1
+                else:
+                    role = 1 + lval
+                shell_info.append((iat, lval, iao, ncart, role))
+                for _ in range(ncart):
+                    index_ctr += [iao] * nprim
+                    iao += 1
+                for m in _MV[lval]:
+                    bas_m += [m] * nprim
+                for k in _KX[lval]:
+                    bas_kx += [k] * nprim
+                for k in _KY[lval]:
+                    bas_ky += [k] * nprim
+                for k in _KZ[lval]:
+                    bas_kz += [k] * nprim
+
+    basis = SimpleNamespace()
+    basis.radial_type = "gto_pure"
+    basis.harmonics_type = "cart"
+    basis.nao = iao
+    nsph = 0
+    for (_, lval, _, _, _) in shell_info:
+        nsph += 2 * lval + 1
+    basis.nmo = nsph
+    basis.nshells = nshells
+    basis.index_ctr = index_ctr
+    intervals = np.concatenate(([0], np.cumsum(nshells)))
+    basis.nao_per_atom = [
+        len(np.unique(index_ctr[intervals[i]:intervals[i + 1]])) for i in range(natm)
+    ]
+    basis.nctr_per_ao = np.array([len(list(g)) for _, g in itertools.groupby(index_ctr)])
+    basis.bas_coeffs = np.array(bas_coeff)
+    basis.bas_exp = np.array(bas_exp)
+    basis.bas_n = bas_n
+    basis.bas_l = bas_l
+    basis.bas_m = bas_m
+    basis.bas_kr = np.zeros_like(basis.bas_exp)
+    basis.bas_kx = np.array(bas_kx)
+    basis.bas_ky = np.array(bas_ky)
+    basis.bas_kz = np.array(bas_kz)
+    basis.bas_norm = norm_gaussian_cartesian(basis.bas_kx, basis.bas_ky, basis.bas_kz,
+                                             basis.bas_exp)
+    basis.atom_coords_internal = np.asarray(atom_coords, dtype=np.float64)
+    basis.TotalEnergy = float("nan")
+    basis._shell_info = shell_info
+    return basis
+
+
+def _overlap_1d(i, j, xpa, xpb, inv2p):
+    """Obara-Saika 1D overlap recursion, table up to (i, j)."""
+    s = np.zeros((i + 1, j + 1))
+    s[0, 0] = 1.0
+    for a in range(i + 1):
+        for b in range(j + 1):
+            if a == 0 and b == 0:
+                continue
+            if a > 0:
+                v = xpa * s[a - 1, b]
+                if a > 1:
+                    v += inv2p * (a - 1) * s[a - 2, b]
+                if b > 0:
+                    v += inv2p * b * s[a - 1, b - 1]
+            else:
+                v = xpb * s[a, b - 1]
+                if b > 1:
+                    v += inv2p * (b - 1) * s[a, b - 2]
+            s[a, b] = v
+    return s[i, j]
+
+
+def ao_overlap(basis, atom_coords):
+    """Overlap matrix of the AOs as evaluated by the AO layer
+    (weights c_p * N_p, entries summed by index_ctr)."""
+    nao = basis.nao
+    centers = np.repeat(np.asarray(atom_coords), basis.nshells, axis=0)
+    w = basis.bas_coeffs * basis.bas_norm
+    k = np.stack([basis.bas_kx, basis.bas_ky, basis.bas_kz], axis=1)
+    idx = np.asarray(basis.index_ctr)
+    S = np.zeros((nao, nao))
+    npr = len(w)
+    for p in range(npr):
+        for q in range(p, npr):
+            a, b = basis.bas_exp[p], basis.bas_exp[q]
+            A, B = centers[p], centers[q]
+            pp = a + b
+            P = (a * A + b * B) / pp
+            kab = math.exp(-a * b / pp * float(np.sum((A - B) ** 2)))
+            val = kab * (math.pi / pp) ** 1.5
+            for d in range(3):
+                val *= _overlap_1d(int(k[p, d]), int(k[q, d]), P[d] - A[d], P[d] - B[d],
+                                   0.5 / pp)
+            val *= w[p] * w[q]
+            S[idx[p], idx[q]] += val
+            if q != p:
+                S[idx[q], idx[p]] += val
+    return S
+
+
+def huckel_mos(basis, atoms, atom_coords, k_wh=1.75):
+    """Extended-Hueckel MOs (lowest ``basis.nmo`` eigenvectors of H C = S C E)."""
+    import scipy.linalg
+
+    S = ao_overlap(basis, atom_coords)
+    hdiag = np.zeros(basis.nao)
+    for (iat, lval, a0, ncomp, role) in basis._shell_info:
+        hdiag[a0:a0 + ncomp] = HUCKEL_VSIE[atoms[iat]][min(role, 3)]
+    H = k_wh * S * 0.5 * (hdiag[:, None] + hdiag[None, :])
+    np.fill_diagonal(H, hdiag * np.diag(S))
+    evals, evecs = scipy.linalg.eigh(H, S)
+    mos = evecs[:, : basis.nmo]
+    # pyscf.py:247 + calculator_base.py:36-46: plain column 2-norm
+    mos = mos / np.sqrt((mos ** 2).sum(0))
+    return mos, evals[: basis.nmo]
+
+
+class Molecule:
+    """Drop-in for ``qmctorch.scf.Molecule`` (``qmctorch/scf/molecule.py:22-162``)
+    restricted to what the hot path reads: ``nelec, nup, ndown, spin, natom,
+    atoms, atomic_number, atomic_nelec, atom_coords, hdf5file, basis``.
+
+    ``calculator`` may be ``"pyscf"`` or ``"builtin"``; both use the built-in
+    tables and the Hueckel MO guess (pyscf is not installed). ``load`` accepts a
+    ``.npz`` file written by :meth:`save`.
+    """
+
+    def __init__(self, atom=None, calculator="pyscf", scf="hf", basis="sto-3g",
+                 unit="bohr", charge=0, spin=0, name=None, load=None,
+                 save_scf_file=False, redo_scf=False, rank=0, mpi_size=0):
+        self.atom_coords = []
+        self.atomic_nelec = []
+        self.atomic_number = []
+        self.atoms = []
+        self.charge = charge
+        self.spin = spin
+        self.unit = unit
+        self.name = name
+        self.basis_name = basis
+        self.calculator_name = calculator
+        self.scf_level = scf
+        self.nelec = 0
+        if load is not None:
+            self._load_npz(load)
+            return
+        if unit not in ("angs", "bohr"):
+            raise ValueError("unit should be angs or bohr")
+        if calculator not in ("pyscf", "builtin"):
+            raise ValueError("only the built-in GTO tables are available (calculator='pyscf')")
+        for a in atom.split(";"):
+            if not a.strip():
+                continue
+            data = a.split()
+            sym = data[0]
+            conv = ANGS2BOHR if unit == "angs" else 1.0
+            self.atoms.append(sym)
+            self.atom_coords.append([float(data[1]) * conv, float(data[2]) * conv,
+                                     float(data[3]) * conv])
+            z = ATOMIC_NUMBER[sym]
+            self.atomic_number.append(z)
+            self.atomic_nelec.append(z)
+            self.nelec += z
+        self.nelec += charge
+        self.natom = len(self.atoms)
+        if (self.nelec - self.spin) % 2 != 0:
+            raise ValueError("%d electrons and spin %d doesn't make sense"
+                             % (self.nelec, self.spin))
+        self.nup = int((self.nelec - self.spin) / 2) + self.spin
+        self.ndown = int((self.nelec - self.spin) / 2)
+        if self.name is None:
+            self.name = "".join(self.atoms)
+        self.hdf5file = "_".join([self.name, calculator, basis]) + ".hdf5"
+        self.basis = build_basis_namespace(self.atoms, self.atom_coords, basis)
+        self.basis.mos, self.basis.mo_energy = huckel_mos(self.basis, self.atoms,
+                                                          self.atom_coords)
+        self.atoms = np.array(self.atoms)
+
+    def domain(self, method):
+        """Walker initialisation domains (``qmctorch/scf/molecule.py:176-214``)."""
+        domain = {"method": method}
+        if method == "center":
+            domain["center"] = np.mean(self.atom_coords, 0)
+        elif method == "uniform":
+            domain["min"] = np.min(self.atom_coords) - 0.5
+            domain["max"] = np.max(self.atom_coords) + 0.5
+        elif method == "normal":
+            domain["mean"] = np.mean(self.atom_coords, 0)
+            domain["sigma"] = np.diag(np.std(self.atom_coords, 0) + 0.25)
+        elif method == "atomic":
+            domain["atom_coords"] = self.atom_coords
+            domain["atom_num"] = self.atomic_number
+            domain["atom_nelec"] = self.atomic_nelec
+        else:
+            raise ValueError("Method to initialize the walkers not recognized")
+        return domain
+
+    _BASIS_KEYS = ("nao", "nmo", "nshells", "index_ctr", "nao_per_atom", "nctr_per_ao",
+                   "bas_coeffs", "bas_exp", "bas_n", "bas_l", "bas_m", "bas_kr", "bas_kx",
+                   "bas_ky", "bas_kz", "bas_norm", "atom_coords_internal", "mos", "TotalEnergy")
+
+    def save(self, filename):
+        """Write the molecule and its basis namespace to ``.npz``."""
+        data = {"mol_" + k: np.asarray(getattr(self, k)) for k in
+                ("atoms", "atom_coords", "atomic_number", "atomic_nelec", "nelec", "nup",
+                 "ndown", "spin", "charge")}
+        for k in self._BASIS_KEYS:
+            data["basis_" + k] = np.asarray(getattr(self.basis, k))
+        data["basis_radial_type"] = np.asarray(self.basis.radial_type)
+        data["basis_harmonics_type"] = np.asarray(self.basis.harmonics_type)
+        np.savez(filename, **data)
+
+    def _load_npz(self, filename):
+        with np.load(filename, allow_pickle=False) as f:
+            self.atoms = f["mol_atoms"].astype("U")
+            self.atom_coords = f["mol_atom_coords"].tolist()
+            self.atomic_number = [int(x) for x in f["mol_atomic_number"]]
+            self.atomic_nelec = [int(x) for x in f["mol_atomic_nelec"]]
+            self.nelec = int(f["mol_nelec"])
+            self.nup = int(f["mol_nup"])
+            self.ndown = int(f["mol_ndown"])
+            self.spin = int(f["mol_spin"])
+            self.charge = int(f["mol_charge"])
+            self.natom = len(self.atoms)
+            self.basis = SimpleNamespace()
+            for k in self._BASIS_KEYS:
+                v = f["basis_" + k]
+                setattr(self.basis, k, v.item() if v.ndim == 0 else v)
+            self.basis.nao = int(self.basis.nao)
+            self.basis.nmo = int(self.basis.nmo)
+            self.basis.radial_type = str(f["basis_radial_type"])
+            self.basis.harmonics_type = str(f["basis_harmonics_type"])
+        self.name = self.name or "".join(self.atoms)
+        self.hdf5file = filename

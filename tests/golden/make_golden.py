@@ -1,0 +1,177 @@
+"""Generate the golden fixtures of the VMC hot path by running the reference
+QMCTorch package itself (FP64, CPU) on seeded inputs.
+
+Usage (in a container where the reference source tree is available):
+
+    python tests/golden/make_golden.py /path/to/QMCTorch
+
+Writes ``tests/golden/<case>.npz``. Each file holds the molecule / basis
+namespace (``mol_*`` / ``basis_*`` keys, the layout of
+``qmctorch_gb300.scf.Molecule.save``), the seeded walker positions and the
+reference outputs: AO values and derivatives, MOs, Jastrow factor and
+derivatives, Slater determinants, psi, pdf, kinetic and local energies, a
+Metropolis replay with injected proposals and uniforms, and the parameter
+gradients of the manual and automatic VMC energy gradients.
+"""
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+sys.path.insert(0, HERE)
+
+import ref_stubs  # noqa: E402
+
+CASES = {
+    # name: (atoms, unit, basis, configs, include_all_mo, nwalkers, random_ci, extras)
+    "h2": ("H 0 0 -0.37; H 0 0 0.37", "angs", "sto-3g", "ground_state", True, 12, False,
+           ("metropolis", "solver")),
+    "lih_cas": ("Li 0 0 0; H 0 0 1.595", "angs", "sto-3g", "cas(2,2)", True, 12, True,
+                ("metropolis", "solver")),
+    "lih_sd": ("Li 0 0 0; H 0 0 3.14", "bohr", "sto-3g", "single_double(2,2)", False, 11, True,
+               ("solver",)),
+    "h2o_sd": ("O 0 0 0.1173; H 0 0.7572 -0.4692; H 0 -0.7572 -0.4692", "angs", "cc-pvdz",
+               "single_double(4,4)", True, 8, True, ("metropolis", "iter", "solver")),
+    "h2o_single": ("O 0 0 0.1173; H 0 0.7572 -0.4692; H 0 -0.7572 -0.4692", "angs", "cc-pvdz",
+                   "single(2,2)", True, 6, True, ()),
+    "h4": ("H 0 0 0; H 0 0 1.0; H 0 0 2.0; H 0 0 3.0", "angs", "sto-3g", "ground_state",
+           False, 8, False, ("metropolis",)),
+    "c6h6": ("C 1.39 0 0; C 0.695 1.20377 0; C -0.695 1.20377 0; C -1.39 0 0; "
+             "C -0.695 -1.20377 0; C 0.695 -1.20377 0; H 2.48 0 0; H 1.24 2.14774 0; "
+             "H -1.24 2.14774 0; H -2.48 0 0; H -1.24 -2.14774 0; H 1.24 -2.14774 0",
+             "angs", "cc-pvdz", "ground_state", True, 3, False, ()),
+}
+
+
+def seeded_positions(mol, nw, seed):
+    """Electrons assigned to atoms in order of their electron count, offset by
+    N(0, 1 bohr^2) per coordinate."""
+    rng = np.random.default_rng(seed)
+    centers = []
+    for iat, ne in enumerate(mol.atomic_nelec):
+        centers += [mol.atom_coords[iat]] * ne
+    centers = np.asarray(centers[: mol.nelec])
+    pos = centers[None] + rng.normal(size=(nw, mol.nelec, 3))
+    return pos.reshape(nw, -1)
+
+
+def main(reference_root):
+    ref_stubs.install(reference_root)
+    import torch
+    from qmctorch.utils import set_torch_double_precision
+    from qmctorch.wavefunction import SlaterJastrow
+    from qmctorch.sampler import Metropolis
+    from qmctorch.solver import Solver
+    import qmctorch.sampler.metropolis as qmet
+    from qmctorch_gb300.scf import Molecule
+
+    set_torch_double_precision()
+    for name, (atoms, unit, basis, configs, all_mo, nw, random_ci, extras) in CASES.items():
+        torch.manual_seed(1234)
+        mol = Molecule(atoms, unit=unit, basis=basis)
+        tmp = os.path.join(HERE, "_tmp_mol.npz")
+        mol.save(tmp)
+        data = dict(np.load(tmp))
+        os.remove(tmp)
+        wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)
+        if random_ci:
+            g = torch.Generator().manual_seed(7)
+            wf.fc.weight.data = torch.rand(wf.fc.weight.shape, generator=g)
+        pos_np = seeded_positions(mol, nw, seed=11)
+        pos = torch.as_tensor(pos_np)
+        data.update(case_configs=np.asarray(configs), case_include_all_mo=np.asarray(all_mo),
+                    fc_weight=wf.fc.weight.detach().numpy().reshape(-1),
+                    jastrow_w=wf.jastrow.jastrow_kernel.weight.detach().numpy(),
+                    pos=pos_np)
+        with torch.no_grad():
+            if name != "c6h6":
+                ao, dao, d2ao = wf.ao(pos, derivative=[0, 1, 2])
+                data.update(ao=ao.numpy(), dao=dao.numpy(), d2ao=d2ao.numpy(),
+                            ao_sumgrad=wf.ao(pos, derivative=1).numpy(),
+                            mo=wf.mo(ao).numpy())
+                jast, djast, d2jast = wf.jastrow(pos, derivative=[0, 1, 2], sum_grad=False)
+                data.update(jast=jast.numpy(), djast=djast.numpy(), d2jast=d2jast.numpy(),
+                            djast_sum=wf.jastrow(pos, derivative=1).numpy(),
+                            dets=wf.pool(wf.mo(ao)).numpy())
+            data.update(psi=wf(pos).numpy(), pdf=wf.pdf(pos).numpy(),
+                        kinetic=wf.kinetic_energy(pos).numpy(),
+                        eloc=wf.local_energy(pos).numpy(),
+                        v_en=wf.nuclear_potential(pos).numpy(),
+                        v_ee=wf.electronic_potential(pos).numpy(),
+                        v_nn=np.asarray(float(wf.nuclear_repulsion())))
+
+        if "metropolis" in extras:
+            rng = np.random.default_rng(21)
+            mnw, nstep, step = 8, 12, 0.2
+            sig = np.sqrt(step / (2 * np.sqrt(2 * np.log(2))))
+            props = rng.normal(size=(nstep, mnw, 3 * mol.nelec)) * sig
+            unif = rng.uniform(size=(nstep, mnw))
+            pos0 = seeded_positions(mol, mnw, seed=5)
+            sampler = Metropolis(nwalkers=mnw, nstep=nstep, step_size=step, ntherm=4,
+                                 ndecor=2, nelec=mol.nelec, init=mol.domain("atomic"),
+                                 move={"type": "all-elec", "proba": "normal"})
+            it_p = iter(torch.as_tensor(props))
+            it_u = iter(torch.as_tensor(unif))
+            sampler._move = types.MethodType(lambda self, n: next(it_p), sampler)
+            orig = qmet.torch.rand_like
+            qmet.torch.rand_like = lambda t: next(it_u).reshape(t.shape).type(t.dtype)
+            try:
+                out = sampler(wf.pdf, pos=torch.tensor(pos0), with_tqdm=False)
+            finally:
+                qmet.torch.rand_like = orig
+            data.update(met_pos0=pos0, met_props=props, met_unif=unif,
+                        met_step=np.asarray(step), met_ntherm=np.asarray(4),
+                        met_ndecor=np.asarray(2), met_out=out.detach().numpy())
+
+        if "iter" in extras:
+            rng = np.random.default_rng(22)
+            mnw, nstep, step = 6, 3, 0.3
+            sig = np.sqrt(step / (2 * np.sqrt(2 * np.log(2))))
+            props = rng.normal(size=(nstep, mol.nelec, mnw, 3)) * sig
+            unif = rng.uniform(size=(nstep, mol.nelec, mnw))
+            pos0 = seeded_positions(mol, mnw, seed=6)
+            sampler = Metropolis(nwalkers=mnw, nstep=nstep, step_size=step, ntherm=-1,
+                                 ndecor=1, nelec=mol.nelec, init=mol.domain("atomic"),
+                                 move={"type": "all-elec-iter", "proba": "normal"})
+            it_p = iter(torch.as_tensor(props.reshape(nstep * mol.nelec, mnw, 3)))
+            it_u = iter(torch.as_tensor(unif.reshape(nstep * mol.nelec, mnw)))
+            sampler._move = types.MethodType(lambda self, n: next(it_p), sampler)
+            orig = qmet.torch.rand_like
+            qmet.torch.rand_like = lambda t: next(it_u).reshape(t.shape).type(t.dtype)
+            try:
+                out = sampler(wf.pdf, pos=torch.tensor(pos0), with_tqdm=False)
+            finally:
+                qmet.torch.rand_like = orig
+            data.update(iter_pos0=pos0, iter_props=props, iter_unif=unif,
+                        iter_out=out.detach().numpy())
+
+        if "solver" in extras:
+            sampler = Metropolis(nwalkers=nw, nstep=2, step_size=0.2, nelec=mol.nelec,
+                                 init=mol.domain("atomic"))
+            opt = torch.optim.Adam(wf.parameters(), lr=1e-3)
+            solver = Solver(wf=wf, sampler=sampler, optimizer=opt, output="_unused.hdf5")
+            names = ["ao.bas_exp", "mo.mo_modifier", "jastrow.jastrow_kernel.weight",
+                     "fc.weight"]
+            params = dict(wf.named_parameters())
+            for mode in ("manual", "auto"):
+                solver.configure(grad=mode, loss="energy", track=["local_energy"])
+                solver.loss.use_weight = False
+                opt.zero_grad()
+                wf.zero_grad()
+                lpos = pos.clone().requires_grad_(mode == "auto")
+                loss, eloc = solver.evaluate_gradient(lpos)
+                data["grad_%s_loss" % mode] = np.asarray(float(loss))
+                for n in names:
+                    g = params[n].grad
+                    data["grad_%s_%s" % (mode, n)] = (np.zeros(params[n].shape) if g is None
+                                                      else g.detach().numpy().copy())
+        out_file = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(out_file, **data)
+        print("wrote", out_file, os.path.getsize(out_file), "bytes")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
