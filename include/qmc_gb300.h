@@ -1,0 +1,217 @@
+/*
+ * qmc_gb300.h -- C ABI of the GB300 (sm_103a) kernels behind the QMCTorch VMC
+ * hot path: Slater-Jastrow wave function values, local energies and
+ * Metropolis sampling.
+ *
+ * The reference (QMCTorch 0.4.0) is pure Python/PyTorch and has no native
+ * interface; each entry point below replaces the reference Python function
+ * cited beside it (paths relative to the QMCTorch repository). A binding
+ * (ctypes, cffi, pybind11) passes plain device pointers and sizes:
+ *
+ *   - every pointer argument is a CUDA device pointer unless stated;
+ *   - FP64 arrays are row-major and contiguous;
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy stream);
+ *   - the caller owns every buffer, including the scratch workspace whose
+ *     size the *_scratch_bytes functions report;
+ *   - calls are asynchronous on `stream`; the return value reports argument
+ *     and launch errors only (0 = QMC_OK).
+ */
+#ifndef QMC_GB300_H
+#define QMC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum qmc_status {
+  QMC_OK = 0,
+  QMC_ERR_ARG = 1,         /* null pointer, negative size, bad mode */
+  QMC_ERR_SHAPE = 2,       /* sizes beyond the compiled limits */
+  QMC_ERR_SCRATCH = 3,     /* scratch buffer too small */
+  QMC_ERR_LAUNCH = 4,      /* CUDA launch / runtime error */
+  QMC_ERR_UNSUPPORTED = 5  /* option not implemented */
+};
+
+/* Compile-time limits of the kernels. */
+#define QMC_MAX_NSPIN 64   /* electrons per spin channel */
+#define QMC_MAX_COMP 6     /* AO components sharing one exponent set */
+
+/* Determinant recipes (SlaterPooling, qmctorch/wavefunction/pooling/slater_pooling.py). */
+#define QMC_DET_EXCITATION 0 /* ground state + single/double excitations via A^-1 B
+                                (det_unique_single_double 147-260,
+                                 operator_unique_single_double 437-636) */
+#define QMC_DET_EXPLICIT 1   /* one LU per unique column set (det_explicit 96-111,
+                                operator_explicit 348-409) */
+
+/*
+ * Wave-function description. Built once per molecule by the host layer from
+ * the basis namespace (AtomicOrbitals.__init__, atomic_orbitals.py:16-102),
+ * the CI configurations (OrbitalConfigurations.get_configs,
+ * orbital_configurations.py:14-63; ExcitationMask, orbital_projector.py:97-189)
+ * and the trainable parameters (ao.bas_exp, mo.mo_modifier,
+ * jastrow.jastrow_kernel.weight, fc.weight), which the kernels read in place.
+ *
+ * AO "groups": consecutive AOs on one atom whose primitive exponents are
+ * identical (cartesian components of a shell, general-contraction columns).
+ * One exp() per (electron, group primitive) serves every AO of the group.
+ */
+typedef struct qmc_wf_desc {
+  int32_t nelec, nup, ndown;
+  int32_t natom;
+  int32_t nao;       /* cartesian AOs */
+  int32_t nmo;       /* columns of mo_scf / mo_modifier */
+  int32_t nmo_used;  /* columns read by the determinants (highest occupied + 1) */
+  int32_t ngroup;    /* AO groups */
+  int32_t ngprim;    /* primitives over all groups */
+  int32_t nweight;   /* AO-primitive weights (= basis entries) */
+  int32_t contract;  /* 0 reproduces the uncontracted-basis value path (atomic_orbitals.py:246-249) */
+  int32_t use_jastrow;
+  /* basis tables */
+  const double* atom_coords;  /* [natom*3] */
+  const double* atom_charge;  /* [natom] */
+  const int32_t* group_atom;  /* [ngroup] */
+  const int32_t* group_prim;  /* [ngroup+1] offsets into the group primitive arrays */
+  const int32_t* group_ao;    /* [ngroup+1] AO ranges */
+  const int32_t* gprim_entry; /* [ngprim] index of the exponent in bas_exp */
+  const double* bas_exp;      /* [nentries] trainable exponents (ao.bas_exp) */
+  const int32_t* ao_k;        /* [nao*3] cartesian powers kx, ky, kz */
+  const int32_t* ao_wofs;     /* [nao] offset of the AO's weights (one per group primitive) */
+  const double* ao_wd;        /* [nweight] bas_coeffs * norm (derivative / contracted path) */
+  const double* ao_wv;        /* [nweight] weights of the value path when contract == 0, else NULL */
+  const double* mo_scf;       /* [nao*nmo] */
+  const double* mo_modifier;  /* [nao*nmo] */
+  /* Jastrow: Pade e-e kernel w0 r / (1 + w r), w0 = 0.25 same spin, 0.5 opposite */
+  const double* jastrow_w;    /* [1] */
+  /* CI expansion */
+  int32_t det_mode;           /* QMC_DET_EXCITATION or QMC_DET_EXPLICIT */
+  int32_t ncfg;
+  int32_t max_orb[2];         /* excitation mode: highest orbital + 1 per spin */
+  int32_t ndet[2];            /* unique spin determinants per spin */
+  const int32_t* det_table[2];/* excitation: [ndet*5] (order, i0, i1, i2, i3) flat indices into
+                                 A^-1 A_virt (n x (max_orb-n)); explicit: [ndet*n] column sets */
+  const int32_t* cfg_det[2];  /* [ncfg] spin determinant of each configuration */
+  const double* ci_weight;    /* [ncfg] (fc.weight) */
+  double e_nuc;               /* nuclear repulsion (wf_base.py:97-116) */
+} qmc_wf_desc;
+
+/* Scratch bytes for nwalkers walkers; kind 0 = psi, 1 = local energy. */
+int64_t qmc_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers, int32_t kind);
+
+/*
+ * psi[w] = J(R_w) * sum_n c_n D_up,n D_down,n for positions pos[nwalkers][3*nelec].
+ * Replaces SlaterJastrow.forward (slater_jastrow.py:243-286) and, squared,
+ * WaveFunction.pdf (wf_base.py:241-247).
+ */
+int qmc_wf_psi(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double* psi,
+               void* scratch, int64_t scratch_bytes, void* stream);
+
+/*
+ * eloc[w] = -1/2 lap(psi)/psi + V_en + V_ee + V_nn; kinetic[w] and psi[w] are
+ * optional (NULL to skip). Replaces WaveFunction.local_energy
+ * (wf_base.py:184-215) with SlaterJastrow.kinetic_energy_jacobi
+ * (slater_jastrow.py:312-344, get_kinetic_operator 449-482).
+ */
+int qmc_wf_local_energy(const qmc_wf_desc* d, const double* pos, int64_t nwalkers,
+                        double* eloc, double* kinetic, double* psi,
+                        void* scratch, int64_t scratch_bytes, void* stream);
+
+/*
+ * AO values. mode 0: ao[nw][ne][nao]; mode 1: gradient dao[nw][ne][nao][3];
+ * mode 2: laplacian d2ao[nw][ne][nao]; mode 3: sum of the gradient components
+ * ao[nw][ne][nao]; mode 4: all of ao, dao, d2ao.
+ * Replaces AtomicOrbitals.forward (atomic_orbitals.py:131-218).
+ */
+int qmc_ao_eval(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, int32_t mode,
+                double* ao, double* dao, double* d2ao, void* stream);
+
+/*
+ * MO values mo[nrows][nmo] = ao[nrows][nao] @ (mo_scf * mo_modifier).
+ * Replaces MolecularOrbitals.forward (molecular_orbitals.py:79-95).
+ */
+int qmc_mo_eval(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* mo, void* stream);
+
+/*
+ * Pade e-e Jastrow. jast[nw] (J), djast[nw][3][ne] (gradient, sum_grad = 0) or
+ * [nw][ne] (sum_grad = 1), d2jast[nw][ne] (laplacian); NULL outputs are skipped.
+ * Replaces JastrowFactorElectronElectron.forward
+ * (jastrow_factor_electron_electron.py:124-260).
+ */
+int qmc_jastrow_ee(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double* jast,
+                   double* djast, double* d2jast, int32_t sum_grad, void* stream);
+
+/*
+ * Slater determinants dets[nw][ncfg] from MO values mo[nw][ne][nmo_ld]
+ * (SlaterPooling.forward, slater_pooling.py:64-80). If bop is not NULL, also
+ * op[nw][ncfg] = Tr(A^-1 B) summed over spins for the operator matrix
+ * bop[nw][ne][nmo_ld] (SlaterPooling.operator, slater_pooling.py:262-306).
+ */
+int qmc_slater(const qmc_wf_desc* d, const double* mo, const double* bop, int32_t nmo_ld,
+               int64_t nwalkers, double* dets, double* op, void* scratch,
+               int64_t scratch_bytes, void* stream);
+
+/*
+ * Coulomb terms per walker: v_en[nw] = -sum_e sum_A Z_A / r_eA and
+ * v_ee[nw] = sum_{i<j} 1 / r_ij (either may be NULL). Replaces
+ * WaveFunction.nuclear_potential / electronic_potential (wf_base.py:49-95).
+ */
+int qmc_potentials(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double* v_en,
+                   double* v_ee, void* stream);
+
+/* Metropolis move types (Metropolis.configure_move, metropolis.py:179-225). */
+#define QMC_MOVE_ALL_ELEC 0
+#define QMC_MOVE_ONE_ELEC 1
+#define QMC_MOVE_ALL_ELEC_ITER 2
+#define QMC_PROBA_NORMAL 0
+#define QMC_PROBA_UNIFORM 1
+
+typedef struct qmc_metropolis_args {
+  double* pos;            /* [nw][3*ne] walker positions, updated in place */
+  int64_t nwalkers;
+  int32_t nstep;
+  int32_t ntherm;         /* >= 0 (the caller resolves negative values) */
+  int32_t ndecor;
+  int32_t move_type;      /* QMC_MOVE_* */
+  int32_t proba;          /* QMC_PROBA_* */
+  double step_size;
+  uint64_t seed;          /* Philox key */
+  uint64_t step_offset;   /* Philox counter offset (continue a chain) */
+  double* samples;        /* [nsnap][nw][3*ne] kept positions, or NULL */
+  int64_t nsnap;          /* capacity of samples in snapshots */
+  int32_t* accepted;      /* [nw] accepted moves, accumulated, or NULL */
+  double* psi_out;        /* [nw] psi at the final positions, or NULL */
+  /* Replay inputs (tests): when not NULL they replace the generator.
+     all-elec: proposals [nstep][nw][3*ne], uniforms [nstep][nw];
+     single-electron: proposals [nstep][nmove][nw][3], uniforms [nstep][nmove][nw],
+     electron_index [nstep][nw] (one-elec). */
+  const double* proposals;
+  const double* uniforms;
+  const int32_t* electron_index;
+} qmc_metropolis_args;
+
+/* Scratch bytes for qmc_metropolis_run. */
+int64_t qmc_metropolis_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
+
+/*
+ * Run nstep Metropolis steps for every walker in one persistent launch.
+ * Replaces Metropolis.__call__ (metropolis.py:85-177) with move / _move /
+ * _accept (227-298): Gaussian proposals of covariance sigma*I with
+ * sigma = step_size / (2 sqrt(2 ln 2)) (quirk kept: per-coordinate standard
+ * deviation sqrt(sigma)) or uniform proposals step*(2u-1); accept when
+ * min(1, psi'^2/psi^2) - u >= 0, zero densities replaced by 1e-16.
+ */
+int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a,
+                       void* scratch, int64_t scratch_bytes, void* stream);
+
+/* Human-readable status. */
+const char* qmc_status_string(int status);
+
+/* Library version string. */
+const char* qmc_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMC_GB300_H */

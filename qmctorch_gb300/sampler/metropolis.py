@@ -1,0 +1,239 @@
+"""Metropolis sampler (drop-in for ``qmctorch.sampler.Metropolis``,
+``qmctorch/sampler/metropolis.py:10-298``) and walkers
+(``qmctorch/sampler/walkers.py:8-150``).
+
+Sampling a wave function of this package runs ``qmc_metropolis_run``: one
+persistent launch in which each thread advances one walker chain through all
+steps (proposal, psi re-evaluation, accept/reject, snapshot), with a Philox
+counter-based generator seeded per sampler. Walker initialisation mirrors the
+reference's host-side RNG calls, so a seeded initial configuration is the
+reference's.
+"""
+from __future__ import annotations
+
+import logging
+import time
+
+import numpy as np
+import torch
+from torch.distributions import MultivariateNormal
+
+from .. import _lib
+from ..wavefunction import runtime as rt
+
+log = logging.getLogger("qmctorch_gb300")
+
+_MOVE = {"all-elec": 0, "one-elec": 1, "all-elec-iter": 2}
+_PROBA = {"normal": 0, "uniform": 1}
+
+
+class Walkers:
+    """Walker positions and their initialisation (walkers.py:8-150)."""
+
+    def __init__(self, nwalkers=100, nelec=1, ndim=3, init=None, cuda=False):
+        self.nwalkers = nwalkers
+        self.ndim = ndim
+        self.nelec = nelec
+        self.init_domain = init
+        self.pos = None
+        self.status = None
+        self.cuda = cuda
+        self.device = torch.device("cuda") if cuda else torch.device("cpu")
+
+    def initialize(self, pos=None):
+        if pos is not None:
+            if len(pos) > self.nwalkers:
+                pos = pos[-self.nwalkers:, :]
+            self.pos = pos
+            return
+        if "center" in self.init_domain:
+            self.pos = self._init_center()
+        elif "min" in self.init_domain:
+            self.pos = self._init_uniform()
+        elif "mean" in self.init_domain:
+            self.pos = self._init_multivar()
+        elif "atom_coords" in self.init_domain:
+            self.pos = self._init_atomic()
+        else:
+            raise ValueError("Init walkers not recognized")
+
+    def _init_center(self):
+        eps = 1e-3
+        pos = -eps + 2 * eps * torch.rand(self.nwalkers, self.nelec * self.ndim)
+        return pos.type(torch.get_default_dtype()).to(device=self.device)
+
+    def _init_uniform(self):
+        pos = torch.rand(self.nwalkers, self.nelec * self.ndim)
+        pos *= self.init_domain["max"] - self.init_domain["min"]
+        pos += self.init_domain["min"]
+        return pos.type(torch.get_default_dtype()).to(device=self.device)
+
+    def _init_multivar(self):
+        multi = MultivariateNormal(torch.as_tensor(self.init_domain["mean"]),
+                                   torch.as_tensor(self.init_domain["sigma"]))
+        pos = multi.sample((self.nwalkers, self.nelec)).type(torch.get_default_dtype())
+        return pos.view(self.nwalkers, self.nelec * self.ndim).to(device=self.device)
+
+    def _init_atomic(self):
+        pos = torch.zeros(self.nwalkers, self.nelec * self.ndim)
+        idx_ref, nelec_tot, natom = [], 0, 0
+        for iat, ne in enumerate(self.init_domain["atom_nelec"]):
+            idx_ref += [iat] * ne
+            nelec_tot += ne
+            natom += 1
+        for iw in range(self.nwalkers):
+            placed = [0] * natom
+            idx = torch.as_tensor(idx_ref)[torch.randperm(nelec_tot)]
+            xyz = torch.as_tensor(self.init_domain["atom_coords"])[idx, :]
+            for ie in range(nelec_tot):
+                i = idx[ie]
+                if placed[i] == 0:
+                    s = 1.0 / self.init_domain["atom_num"][i]
+                elif placed[i] < 5:
+                    s = 2.0 / (self.init_domain["atom_num"][i] - 2)
+                else:
+                    s = 3.0 / (self.init_domain["atom_num"][i] - 3)
+                xyz[ie, :] += np.random.normal(scale=s, size=(1, 3))
+                placed[i] += 1
+            pos[iw, :] = xyz.view(-1)
+        return pos.to(device=self.device)
+
+
+class SamplerBase:
+    """sampler_base.py:7-91."""
+
+    def __init__(self, nwalkers, nstep, step_size, ntherm, ndecor, nelec, ndim, init, cuda):
+        self.nelec = nelec
+        self.ndim = ndim
+        self.nstep = nstep
+        self.step_size = step_size
+        self.ntherm = ntherm
+        self.ndecor = ndecor
+        self.cuda = cuda
+        self.device = torch.device("cuda") if cuda else torch.device("cpu")
+        self.walkers = Walkers(nwalkers=nwalkers, nelec=nelec, ndim=ndim, init=init, cuda=cuda)
+
+    def __repr__(self):
+        return self.__class__.__name__ + " sampler with  %d walkers" % self.walkers.nwalkers
+
+    def get_sampling_size(self):
+        if self.ntherm == -1:
+            return self.walkers.nwalkers
+        return self.walkers.nwalkers * int((self.nstep - self.ntherm) / self.ndecor)
+
+
+class Metropolis(SamplerBase):
+    def __init__(self, nwalkers=100, nstep=1000, step_size=0.2, ntherm=-1, ndecor=1, nelec=1,
+                 ndim=3, init={"min": -5, "max": 5}, move={"type": "all-elec", "proba": "normal"},
+                 logspace=False, symmetry=None, cuda=False, seed=None):
+        SamplerBase.__init__(self, nwalkers, nstep, step_size, ntherm, ndecor, nelec, ndim, init,
+                             cuda)
+        self.logspace = logspace
+        self.configure_move(move)
+        self.symmetry = (lambda x: x) if symmetry is None else symmetry
+        if seed is None:
+            seed = int(torch.randint(0, 2 ** 62, (1,)).item())
+        self.seed = int(seed)
+        self._step_counter = 0
+        self.last_acceptance = None
+
+    def configure_move(self, move):
+        """metropolis.py:179-225."""
+        self.movedict = move
+        if "type" not in self.movedict:
+            self.movedict["type"] = "one-elec"
+        if "proba" not in self.movedict:
+            self.movedict["proba"] = "uniform"
+        if self.movedict["type"] not in _MOVE:
+            raise ValueError(" 'type' in move should be 'one-elec','all-elec', 'all-elec-iter'")
+        if self.movedict["proba"] not in _PROBA:
+            raise ValueError("'proba' in move should be 'normal' or 'uniform'")
+        self._move_per_iter = self.nelec if self.movedict["type"] == "all-elec-iter" else 1
+        self.fixed_id_elec_list = (range(self.nelec) if self.movedict["type"] == "all-elec-iter"
+                                   else [None])
+
+    def _wavefunction(self, pdf):
+        wf = getattr(pdf, "__self__", None)
+        from ..wavefunction.slater_jastrow import SlaterJastrow
+        if not isinstance(wf, SlaterJastrow) or getattr(pdf, "__name__", "") != "pdf":
+            raise TypeError("Metropolis samples the pdf of a qmctorch_gb300 wave function: "
+                            "pass wf.pdf")
+        return wf
+
+    def nsnap(self):
+        ntherm = self.ntherm if self.ntherm >= 0 else self.nstep + self.ntherm
+        return len(range(ntherm, self.nstep, self.ndecor))
+
+    def __call__(self, pdf, pos=None, with_tqdm=True, replay=None):
+        """Sample ``pdf`` (= wf.pdf); returns the kept positions
+        (nsnap * nwalkers, 3 * nelec) (metropolis.py:85-177).
+
+        ``replay`` (tests) = dict(proposals=..., uniforms=..., electron_index=...)
+        replaces the generator with the caller's random numbers, in the
+        layouts of ``qmc_metropolis_args``."""
+        wf = self._wavefunction(pdf)
+        if self.ntherm >= self.nstep:
+            raise ValueError("Thermalisation longer than trajectory")
+        if self.ntherm < 0:
+            self.ntherm = self.nstep + self.ntherm
+        device = rt.cuda_device()
+        out_device = pos.device if pos is not None else (
+            torch.device("cuda") if self.cuda else torch.device("cpu"))
+        out_dtype = pos.dtype if pos is not None else torch.get_default_dtype()
+        with torch.no_grad():
+            self.walkers.initialize(pos=pos)
+            x = rt.dev64(self.walkers.pos, device).clone()
+            nw = x.shape[0]
+            nsnap = len(range(self.ntherm, self.nstep, self.ndecor))
+            samples = torch.empty((max(nsnap, 1), nw, self.nelec * self.ndim), dtype=rt.F64,
+                                  device=device)
+            acc = torch.zeros(nw, dtype=torch.int32, device=device)
+            call = wf._desc(device)
+            lib = _lib.lib()
+            scr = rt.scratch(lib.qmc_metropolis_scratch_bytes(call.ref, nw), device)
+            a = _lib.MetropolisArgs()
+            a.pos = rt.ptr(x)
+            a.nwalkers = nw
+            a.nstep = self.nstep
+            a.ntherm = self.ntherm
+            a.ndecor = self.ndecor
+            a.move_type = _MOVE[self.movedict["type"]]
+            a.proba = _PROBA[self.movedict["proba"]]
+            a.step_size = float(self.step_size)
+            a.seed = self.seed
+            a.step_offset = self._step_counter
+            a.samples = rt.ptr(samples)
+            a.nsnap = nsnap
+            a.accepted = rt.ptr(acc)
+            a.psi_out = None
+            keep = []
+            if replay is not None:
+                props = rt.dev64(replay["proposals"], device)
+                unif = rt.dev64(replay["uniforms"], device)
+                keep += [props, unif]
+                a.proposals, a.uniforms = rt.ptr(props), rt.ptr(unif)
+                if replay.get("electron_index") is not None:
+                    ei = torch.as_tensor(replay["electron_index"]).to(device, torch.int32).contiguous()
+                    keep.append(ei)
+                    a.electron_index = rt.ptr(ei)
+            tstart = time.time()
+            _lib.check(lib.qmc_metropolis_run(call.ref, a, rt.ptr(scr), scr.numel(),
+                                              rt.stream_handle()), "qmc_metropolis_run")
+            self._step_counter += self.nstep
+            # the reference updates the walker tensor (and so a caller's pos) in place
+            wp = self.walkers.pos
+            if wp.shape == x.shape:
+                wp.data.copy_(x.to(device=wp.device, dtype=wp.dtype))
+            else:
+                self.walkers.pos = x.to(device=wp.device, dtype=out_dtype)
+            if with_tqdm:
+                rate = float(acc.sum()) / (nw * self._move_per_iter * self.nstep)
+                self.last_acceptance = rate
+                dt = time.time() - tstart
+                log.info("   Acceptance rate     : %1.2f %%", rate * 100)
+                log.info("   Timing statistics   : %1.2f steps/sec.", self.nstep / dt)
+                log.info("   Total Time          : %1.2f sec.", dt)
+            self._last_accepted = acc
+            out = samples[:nsnap].reshape(nsnap * nw, -1)
+        out = out.to(device=out_device, dtype=out_dtype)
+        return self.symmetry(out).requires_grad_()

@@ -1,0 +1,134 @@
+"""Call plumbing between the torch modules and ``libqmc_gb300``: device
+placement, the ``qmc_wf_desc`` of each call and scratch buffers.
+
+The kernels compute in FP64 on the current CUDA device. Inputs on another
+device or dtype are copied for the call and outputs are returned on the
+input's device and dtype, so the modules accept the CPU tensors the reference
+API is usually called with.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import torch
+
+from .. import _lib
+
+F64 = torch.float64
+
+
+def cuda_device():
+    if not torch.cuda.is_available():
+        raise RuntimeError("qmctorch_gb300 runs its kernels on a CUDA GPU (sm_103a); "
+                           "no CUDA device is visible")
+    return torch.device("cuda", torch.cuda.current_device())
+
+
+def dev64(t, device):
+    """Contiguous FP64 copy of ``t`` on ``device`` (no copy if already there)."""
+    t = t.detach() if isinstance(t, torch.Tensor) else torch.as_tensor(t)
+    if t.device != device or t.dtype != F64 or not t.is_contiguous():
+        t = t.to(device=device, dtype=F64).contiguous()
+    return t
+
+
+def ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def stream_handle():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+_DUMMY = {}
+
+
+def dummies(device):
+    key = str(device)
+    if key not in _DUMMY:
+        _DUMMY[key] = (torch.zeros(8, dtype=torch.int32, device=device),
+                       torch.ones(8, dtype=F64, device=device))
+    return _DUMMY[key]
+
+
+def scratch(nbytes, device):
+    return torch.empty(max(int(nbytes), 8), dtype=torch.uint8, device=device)
+
+
+class Call:
+    """A filled ``qmc_wf_desc`` plus the tensors its pointers refer to."""
+
+    def __init__(self, desc, keep):
+        self.desc = desc
+        self.keep = keep
+        self.ref = ctypes.byref(desc)
+
+
+def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None, nup=None,
+               ndown=None, nmo_used=None, e_nuc=0.0):
+    """Fill a ``qmc_wf_desc`` from the modules of a wave function. Any module
+    may be absent (a standalone AO or Jastrow call); its fields then point to
+    placeholders the called kernel does not read."""
+    di, dd = dummies(device)
+    keep = [di, dd]
+    d = _lib.WfDesc()
+    nelec = ao.nelec if nelec is None else nelec
+    d.nelec = nelec
+    d.nup = nelec if nup is None else nup
+    d.ndown = 0 if ndown is None else ndown
+    d.natom = ao.natoms
+    d.nao = ao.norb
+    bt = ao.device_tables(device)
+    coords = dev64(ao.atom_coords, device)
+    charge = ao.atomic_charge(device)
+    bexp = dev64(ao.bas_exp, device)
+    keep += [coords, charge, bexp]
+    d.ngroup, d.ngprim, d.nweight = bt.ngroup, bt.ngprim, bt.nweight
+    d.contract = int(bt.contract)
+    d.atom_coords, d.atom_charge = ptr(coords), ptr(charge)
+    t = bt.t
+    d.group_atom, d.group_prim, d.group_ao = ptr(t["group_atom"]), ptr(t["group_prim"]), ptr(
+        t["group_ao"])
+    d.gprim_entry, d.bas_exp, d.ao_k = ptr(t["gprim_entry"]), ptr(bexp), ptr(t["ao_k"])
+    d.ao_wofs, d.ao_wd = ptr(t["ao_wofs"]), ptr(t["ao_wd"])
+    d.ao_wv = ptr(t["ao_wv"]) if not bt.contract else None
+    if mo is not None:
+        scf = dev64(mo.mo_scf, device)
+        mod = dev64(mo.mo_modifier, device)
+        keep += [scf, mod]
+        d.nmo = scf.shape[1]
+        d.mo_scf, d.mo_modifier = ptr(scf), ptr(mod)
+    else:
+        d.nmo = 1
+        d.mo_scf = d.mo_modifier = ptr(dd)
+    d.nmo_used = d.nmo if nmo_used is None else nmo_used
+    if jastrow is not None:
+        wj = dev64(jastrow.jastrow_kernel.weight, device)
+        keep.append(wj)
+        d.use_jastrow = 1
+        d.jastrow_w = ptr(wj)
+    else:
+        d.use_jastrow = 0
+        d.jastrow_w = ptr(dd)
+    if pool is not None:
+        ct = pool.device_tables(device)
+        d.det_mode = 1 if ct.explicit else 0
+        d.ncfg = ct.ncfg
+        d.max_orb[0], d.max_orb[1] = ct.max_orb
+        d.ndet[0], d.ndet[1] = ct.ndet
+        d.det_table[0], d.det_table[1] = ptr(ct.t["det_table0"]), ptr(ct.t["det_table1"])
+        d.cfg_det[0], d.cfg_det[1] = ptr(ct.t["cfg_det0"]), ptr(ct.t["cfg_det1"])
+    else:
+        d.det_mode, d.ncfg = 0, 1
+        d.max_orb[0], d.max_orb[1] = d.nup, d.ndown
+        d.ndet[0] = d.ndet[1] = 1
+        d.det_table[0] = d.det_table[1] = ptr(di)
+        d.cfg_det[0] = d.cfg_det[1] = ptr(di)
+    if fc is not None:
+        cw = dev64(fc.weight.reshape(-1), device)
+        keep.append(cw)
+        d.ci_weight = ptr(cw)
+    else:
+        d.ci_weight = ptr(dd)
+    d.e_nuc = float(e_nuc)
+    return Call(d, keep)

@@ -1,0 +1,124 @@
+"""GPU parity of the sm_103a kernels (through the C ABI) with the reference
+outputs stored in the golden fixtures and with the CPU oracle.
+
+Tolerance: FP64, 1e-10 relative on psi, E_L and every intermediate (the bar
+the hot path is held to), with an absolute floor of 1e-12 times the largest
+magnitude of the compared array for values that cancel to ~0.
+"""
+import numpy as np
+import pytest
+import torch
+
+from oracle import qmc_oracle as orc
+from tests.golden_cases import CASES, load
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-10
+
+
+def close(a, b, rtol=RTOL, floor=1e-12):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    atol = floor * max(1.0, float(np.abs(b).max()))
+    np.testing.assert_allclose(a, b, rtol=rtol, atol=atol)
+
+
+def make_wf(mol, d):
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    torch.set_default_dtype(torch.float64)
+    wf = SlaterJastrow(mol, configs=d["configs"], include_all_mo=d["include_all_mo"], cuda=True)
+    wf.fc.weight.data = torch.as_tensor(d["fc_weight"]).reshape(1, -1).to(wf.fc.weight.device)
+    return wf
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_psi_and_local_energy(name):
+    mol, d = load(name)
+    wf = make_wf(mol, d)
+    pos = torch.as_tensor(d["pos"]).cuda()
+    close(wf(pos), d["psi"])
+    close(wf.pdf(pos), d["pdf"])
+    close(wf.kinetic_energy(pos), d["kinetic"])
+    close(wf.local_energy(pos), d["eloc"])
+    close(wf.nuclear_potential(pos), d["v_en"])
+    close(wf.electronic_potential(pos), d["v_ee"])
+    assert abs(wf.nuclear_repulsion() - float(d["v_nn"])) < 1e-12 * max(1, abs(float(d["v_nn"])))
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if c != "c6h6"])
+def test_staged_modules(name):
+    mol, d = load(name)
+    wf = make_wf(mol, d)
+    pos = torch.as_tensor(d["pos"]).cuda()
+    ao, dao, d2ao = wf.ao(pos, derivative=[0, 1, 2])
+    close(ao, d["ao"])
+    close(dao, d["dao"])
+    close(d2ao, d["d2ao"])
+    close(wf.ao(pos), d["ao"])
+    close(wf.ao(pos, derivative=1), d["ao_sumgrad"])
+    close(wf.ao(pos, derivative=1, sum_grad=False), d["dao"])
+    close(wf.ao(pos, derivative=2), d["d2ao"])
+    mo = wf.mo(ao)
+    close(mo, d["mo"])
+    j, dj, d2j = wf.jastrow(pos, derivative=[0, 1, 2], sum_grad=False)
+    close(j, d["jast"])
+    close(dj, d["djast"])
+    close(d2j, d["d2jast"])
+    close(wf.jastrow(pos, derivative=1), d["djast_sum"])
+    close(wf.pool(mo), d["dets"], rtol=1e-9)
+    close(wf(pos, ao=ao), d["psi"], rtol=1e-9)
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_psi_matches_oracle_on_fresh_positions(name):
+    mol, d = load(name)
+    wf = make_wf(mol, d)
+    ow = orc.OracleSlaterJastrow(mol, configs=d["configs"], include_all_mo=d["include_all_mo"],
+                                 fc_weight=d["fc_weight"])
+    rng = np.random.default_rng(99)
+    nw = 4 if name == "c6h6" else 33  # ragged: not a multiple of the block size
+    pos = d["pos"][rng.integers(0, len(d["pos"]), nw)] + 0.3 * rng.normal(size=(nw, d["pos"].shape[1]))
+    x = torch.as_tensor(pos).cuda()
+    close(wf(x), ow.forward(pos), rtol=1e-9)
+    close(wf.local_energy(x), ow.local_energy(pos), rtol=1e-9)
+
+
+def test_empty_batch():
+    mol, d = load("h2")
+    wf = make_wf(mol, d)
+    x = torch.zeros((0, 6), dtype=torch.float64, device="cuda")
+    assert wf(x).shape == (0, 1)
+    assert wf.local_energy(x).shape == (0, 1)
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if "met_out" in load(c)[1]])
+def test_metropolis_replay(name):
+    """Same proposals and uniforms -> same accept/reject decisions and the same
+    kept positions as the reference sampler."""
+    from qmctorch_gb300.sampler import Metropolis
+    mol, d = load(name)
+    wf = make_wf(mol, d)
+    props, unif = d["met_props"], d["met_unif"]
+    nstep, nw = unif.shape
+    sampler = Metropolis(nwalkers=nw, nstep=nstep, step_size=float(d["met_step"]),
+                         ntherm=int(d["met_ntherm"]), ndecor=int(d["met_ndecor"]), nelec=mol.nelec,
+                         init=mol.domain("atomic"), cuda=True)
+    out = sampler(wf.pdf, pos=torch.as_tensor(d["met_pos0"]).cuda(), with_tqdm=False,
+                  replay={"proposals": props, "uniforms": unif})
+    close(out, d["met_out"], rtol=1e-12)
+
+
+def test_metropolis_iter_replay():
+    from qmctorch_gb300.sampler import Metropolis
+    mol, d = load("h2o_sd")
+    wf = make_wf(mol, d)
+    props, unif = d["iter_props"], d["iter_unif"]
+    nstep, nmove, nw = unif.shape
+    sampler = Metropolis(nwalkers=nw, nstep=nstep, step_size=0.3, ntherm=-1, ndecor=1,
+                         nelec=mol.nelec, init=mol.domain("atomic"),
+                         move={"type": "all-elec-iter", "proba": "normal"}, cuda=True)
+    out = sampler(wf.pdf, pos=torch.as_tensor(d["iter_pos0"]).cuda(), with_tqdm=False,
+                  replay={"proposals": props, "uniforms": unif})
+    close(out, d["iter_out"], rtol=1e-12)

@@ -1,0 +1,157 @@
+"""CPU tests: the C ABI library loads and exports what the header declares,
+and the host-side table builders agree with the oracle's restatement of the
+reference index logic."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import qmc_oracle as orc
+from qmctorch_gb300 import _lib
+from qmctorch_gb300.scf import Molecule
+from qmctorch_gb300.wavefunction import SlaterJastrow
+from qmctorch_gb300.wavefunction.tables import BasisTables, ConfigTables, OrbitalConfigurations
+from tests.golden_cases import CASES, load
+
+HEADER = os.path.join(_lib.ROOT, "include", "qmc_gb300.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(qmc_\w+)\s*\(", src)))
+
+
+def test_library_exports_every_header_symbol():
+    lib = _lib.lib()
+    names = header_functions()
+    assert len(names) >= 10
+    for n in names:
+        assert hasattr(lib, n), n
+        assert n in _lib.SIGNATURES, n
+    assert lib.qmc_version().startswith(b"qmc_gb300")
+
+
+def test_struct_layout_matches_header_order():
+    src = open(HEADER).read()
+    body = src[src.index("typedef struct qmc_wf_desc"):src.index("} qmc_wf_desc;")]
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = []
+    for decl in body.split(";")[:-1]:
+        decl = decl.split("{")[-1]
+        for part in decl.split(","):
+            m = re.search(r"(\w+)\s*(\[\d\])?\s*$", part.strip())
+            if m:
+                fields.append(m.group(1))
+    assert fields == [f[0] for f in _lib.WfDesc._fields_]
+
+
+def _desc_for(name):
+    mol, d = load(name)
+    wf = SlaterJastrow(mol, configs=d["configs"], include_all_mo=d["include_all_mo"])
+    keep = []
+
+    def p(t):
+        t = t.detach().contiguous()
+        keep.append(t)
+        return ctypes.c_void_p(t.data_ptr())
+
+    desc = _lib.WfDesc()
+    bt, ct = wf.ao._tables, wf.pool._tables
+    desc.nelec, desc.nup, desc.ndown = mol.nelec, mol.nup, mol.ndown
+    desc.natom, desc.nao, desc.nmo = mol.natom, mol.basis.nao, wf.mo.mo_scf.shape[1]
+    desc.nmo_used = wf.highest_occ_mo
+    desc.ngroup, desc.ngprim, desc.nweight, desc.contract = bt.ngroup, bt.ngprim, bt.nweight, 1
+    desc.use_jastrow = 1
+    for f in ("atom_coords", "atom_charge", "bas_exp", "mo_scf", "mo_modifier", "jastrow_w",
+              "ci_weight"):
+        setattr(desc, f, p(torch.ones(4)))
+    for f in ("group_atom", "group_prim", "group_ao", "gprim_entry", "ao_k", "ao_wofs"):
+        setattr(desc, f, p(bt.t[f]))
+    desc.ao_wd = p(bt.t["ao_wd"])
+    desc.det_mode = int(ct.explicit)
+    desc.ncfg = ct.ncfg
+    desc.max_orb[0], desc.max_orb[1] = ct.max_orb
+    desc.ndet[0], desc.ndet[1] = ct.ndet
+    desc.det_table[0], desc.det_table[1] = p(ct.t["det_table0"]), p(ct.t["det_table1"])
+    desc.cfg_det[0], desc.cfg_det[1] = p(ct.t["cfg_det0"]), p(ct.t["cfg_det1"])
+    return desc, keep, wf
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_scratch_sizes_and_argument_checks(name):
+    lib = _lib.lib()
+    desc, keep, wf = _desc_for(name)
+    b0 = lib.qmc_scratch_bytes(ctypes.byref(desc), 1000, 0)
+    b1 = lib.qmc_scratch_bytes(ctypes.byref(desc), 1000, 1)
+    bm = lib.qmc_metropolis_scratch_bytes(ctypes.byref(desc), 1000)
+    assert 0 < b0 < b1 and b0 < bm
+    assert b0 % (8 * 1024) == 0  # 1000 walkers padded to 1024 slots
+    # argument errors are reported, never launched (no GPU needed)
+    assert lib.qmc_wf_psi(ctypes.byref(desc), None, 10, None, None, 0, None) == 1
+    assert lib.qmc_wf_psi(ctypes.byref(desc), ctypes.c_void_p(8), 10, ctypes.c_void_p(8),
+                          ctypes.c_void_p(8), 8, None) == 3
+    assert lib.qmc_wf_psi(None, None, 0, None, None, 0, None) == 1
+    desc.nup = 100
+    desc.nelec = 100 + desc.ndown
+    assert lib.qmc_wf_psi(ctypes.byref(desc), None, 0, None, None, 0, None) == 2
+    assert lib.qmc_status_string(3) == b"scratch buffer too small"
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_config_tables_match_oracle(name):
+    mol, d = load(name)
+    oc = OrbitalConfigurations(mol).get_configs(d["configs"])
+    cu, cd = orc.get_configs(d["configs"], mol.nup, mol.ndown, mol.basis.nmo)
+    assert np.array_equal(oc[0].numpy(), cu) and np.array_equal(oc[1].numpy(), cd)
+    ct = ConfigTables(d["configs"], oc, mol.nup, mol.ndown)
+    op = orc.OraclePool(d["configs"], (cu, cd), mol.nup, mol.ndown)
+    if op.explicit:
+        assert np.array_equal(ct.t["det_table0"].numpy().reshape(-1, mol.nup), op.ucfg_up)
+        assert np.array_equal(ct.t["cfg_det0"].numpy(), op.iucfg_up)
+        assert np.array_equal(ct.t["cfg_det1"].numpy(), op.iucfg_dn)
+    else:
+        tab = ct.t["det_table0"].numpy().reshape(-1, 5)
+        assert [int(r[1]) for r in tab if r[0] == 1] == op.single_up
+        assert [int(x) for r in tab if r[0] == 2 for x in r[1:]] == op.double_up
+        tab = ct.t["det_table1"].numpy().reshape(-1, 5)
+        assert [int(r[1]) for r in tab if r[0] == 1] == op.single_dn
+        assert np.array_equal(ct.t["cfg_det0"].numpy(), op.index_unique_exc[0])
+        assert np.array_equal(ct.t["cfg_det1"].numpy(), op.index_unique_exc[1])
+
+
+def test_basis_groups_share_exponents():
+    mol, _ = load("h2o_sd")
+    bt = BasisTables(mol.basis, mol.basis.bas_exp)
+    assert bt.nweight == len(mol.basis.bas_exp) == 56
+    assert bt.ngprim == 28 and bt.ngroup == 11
+    ga = bt.t["group_ao"].numpy()
+    assert ga[-1] == mol.basis.nao and np.all(np.diff(ga) <= 6)
+    # training that splits a group regroups
+    e = np.array(mol.basis.bas_exp, dtype=np.float64)
+    e[-1] *= 1.01  # last d component of the last atom group
+    assert not bt.still_valid(e)
+    bt2 = BasisTables(mol.basis, e)
+    assert bt2.ngroup > bt.ngroup
+
+
+def test_molecule_roundtrip(tmp_path):
+    mol = Molecule("Li 0 0 0; H 0 0 1.595", unit="angs", basis="sto-3g")
+    f = str(tmp_path / "lih.npz")
+    mol.save(f)
+    m2 = Molecule(load=f)
+    assert m2.nelec == 4 and m2.nup == 2 and m2.basis.nao == 6
+    assert np.allclose(m2.basis.mos, mol.basis.mos)
+    assert mol.domain("atomic")["atom_nelec"] == [3, 1]
+
+
+def test_missing_gpu_fails_loudly():
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    mol, d = load("h2")
+    wf = SlaterJastrow(mol)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        wf(torch.zeros(2, 6))
