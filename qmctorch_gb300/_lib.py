@@ -22,7 +22,8 @@ LIBPATH = os.path.join(LIBDIR, "libqmc_gb300.so")
 BUILD = os.path.join(ROOT, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
-SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu"]
+SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
+           "qmc_probe.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 
@@ -36,7 +37,7 @@ def _nvcc():
 
 def _deps_mtime():
     files = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    files.append(os.path.join(INCLUDE, "qmc_gb300.h"))
+    files += [os.path.join(INCLUDE, f) for f in os.listdir(INCLUDE)]
     return max(os.path.getmtime(f) for f in files)
 
 
@@ -126,6 +127,7 @@ SIGNATURES = {
                                   c_void_p, c_void_p, c_int64, c_void_p]),
     "qmc_potentials": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                       c_void_p]),
+    "qmc_probe_fma": (ctypes.c_int, [c_int32, c_int32, c_int64, c_void_p, c_void_p]),
     "qmc_metropolis_run": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), c_void_p, c_int64,
                                           c_void_p]),
 }

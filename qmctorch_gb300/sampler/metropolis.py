@@ -164,6 +164,57 @@ class Metropolis(SamplerBase):
         ntherm = self.ntherm if self.ntherm >= 0 else self.nstep + self.ntherm
         return len(range(ntherm, self.nstep, self.ndecor))
 
+    def _run_kernel(self, wf, x, device, samples=None, nsnap=0, accepted=None, replay=None,
+                    nstep=None, ntherm=None, scratch=None):
+        """One ``qmc_metropolis_run`` launch on the current stream; ``x``
+        (nw, 3*nelec) FP64 on ``device`` is advanced in place."""
+        nw = x.shape[0]
+        call = wf._desc(device)
+        lib = _lib.lib()
+        need = lib.qmc_metropolis_scratch_bytes(call.ref, nw)
+        scr = scratch if (scratch is not None and scratch.numel() >= need) else rt.scratch(need,
+                                                                                         device)
+        nstep = self.nstep if nstep is None else nstep
+        a = _lib.MetropolisArgs()
+        a.pos = rt.ptr(x)
+        a.nwalkers = nw
+        a.nstep = nstep
+        a.ntherm = (self.ntherm if ntherm is None else ntherm)
+        a.ndecor = self.ndecor
+        a.move_type = _MOVE[self.movedict["type"]]
+        a.proba = _PROBA[self.movedict["proba"]]
+        a.step_size = float(self.step_size)
+        a.seed = self.seed
+        a.step_offset = self._step_counter
+        a.samples = rt.ptr(samples)
+        a.nsnap = nsnap
+        a.accepted = rt.ptr(accepted)
+        a.psi_out = None
+        keep = [scr]
+        if replay is not None:
+            props = rt.dev64(replay["proposals"], device)
+            unif = rt.dev64(replay["uniforms"], device)
+            keep += [props, unif]
+            a.proposals, a.uniforms = rt.ptr(props), rt.ptr(unif)
+            if replay.get("electron_index") is not None:
+                ei = torch.as_tensor(replay["electron_index"]).to(device, torch.int32).contiguous()
+                keep.append(ei)
+                a.electron_index = rt.ptr(ei)
+        _lib.check(lib.qmc_metropolis_run(call.ref, a, rt.ptr(scr), scr.numel(),
+                                          rt.stream_handle()), "qmc_metropolis_run")
+        return keep
+
+    def advance(self, pdf, x, nstep=None, accepted=None, scratch=None):
+        """Device-resident sampling: advance the walkers ``x`` (CUDA FP64,
+        (nw, 3*nelec)) by ``nstep`` Metropolis steps in place, keeping no
+        snapshots. Launches exactly one kernel."""
+        wf = self._wavefunction(pdf)
+        nstep = self.nstep if nstep is None else nstep
+        keep = self._run_kernel(wf, x, x.device, accepted=accepted, nstep=nstep, ntherm=nstep,
+                                scratch=scratch)
+        self._step_counter += nstep
+        return keep
+
     def __call__(self, pdf, pos=None, with_tqdm=True, replay=None):
         """Sample ``pdf`` (= wf.pdf); returns the kept positions
         (nsnap * nwalkers, 3 * nelec) (metropolis.py:85-177).
@@ -188,37 +239,9 @@ class Metropolis(SamplerBase):
             samples = torch.empty((max(nsnap, 1), nw, self.nelec * self.ndim), dtype=rt.F64,
                                   device=device)
             acc = torch.zeros(nw, dtype=torch.int32, device=device)
-            call = wf._desc(device)
-            lib = _lib.lib()
-            scr = rt.scratch(lib.qmc_metropolis_scratch_bytes(call.ref, nw), device)
-            a = _lib.MetropolisArgs()
-            a.pos = rt.ptr(x)
-            a.nwalkers = nw
-            a.nstep = self.nstep
-            a.ntherm = self.ntherm
-            a.ndecor = self.ndecor
-            a.move_type = _MOVE[self.movedict["type"]]
-            a.proba = _PROBA[self.movedict["proba"]]
-            a.step_size = float(self.step_size)
-            a.seed = self.seed
-            a.step_offset = self._step_counter
-            a.samples = rt.ptr(samples)
-            a.nsnap = nsnap
-            a.accepted = rt.ptr(acc)
-            a.psi_out = None
-            keep = []
-            if replay is not None:
-                props = rt.dev64(replay["proposals"], device)
-                unif = rt.dev64(replay["uniforms"], device)
-                keep += [props, unif]
-                a.proposals, a.uniforms = rt.ptr(props), rt.ptr(unif)
-                if replay.get("electron_index") is not None:
-                    ei = torch.as_tensor(replay["electron_index"]).to(device, torch.int32).contiguous()
-                    keep.append(ei)
-                    a.electron_index = rt.ptr(ei)
             tstart = time.time()
-            _lib.check(lib.qmc_metropolis_run(call.ref, a, rt.ptr(scr), scr.numel(),
-                                              rt.stream_handle()), "qmc_metropolis_run")
+            self._run_kernel(wf, x, device, samples=samples, nsnap=nsnap, accepted=acc,
+                             replay=replay)
             self._step_counter += self.nstep
             # the reference updates the walker tensor (and so a caller's pos) in place
             wp = self.walkers.pos

@@ -17,12 +17,16 @@ from qmctorch_gb300.wavefunction.tables import BasisTables, ConfigTables, Orbita
 from tests.golden_cases import CASES, load
 
 HEADER = os.path.join(_lib.ROOT, "include", "qmc_gb300.h")
+INCLUDE = os.path.join(_lib.ROOT, "include")
 
 
 def header_functions():
-    src = open(HEADER).read()
-    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
-    return sorted(set(re.findall(r"\b(qmc_\w+)\s*\(", src)))
+    names = set()
+    for f in os.listdir(INCLUDE):
+        src = open(os.path.join(INCLUDE, f)).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        names |= set(re.findall(r"\b(qmc_\w+)\s*\(", src))
+    return sorted(names)
 
 
 def test_library_exports_every_header_symbol():
