@@ -31,7 +31,8 @@ enum qmc_status {
   QMC_ERR_SHAPE = 2,       /* sizes beyond the compiled limits */
   QMC_ERR_SCRATCH = 3,     /* scratch buffer too small */
   QMC_ERR_LAUNCH = 4,      /* CUDA launch / runtime error */
-  QMC_ERR_UNSUPPORTED = 5  /* option not implemented */
+  QMC_ERR_UNSUPPORTED = 5, /* option not implemented */
+  QMC_ERR_STATIC_LIMIT = 6 /* batch needs more than QMC_STATIC_SCRATCH_BYTES (qmc_wf_psi_static) */
 };
 
 /* Compile-time limits of the kernels. */
@@ -106,6 +107,34 @@ int64_t qmc_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers, int32_t kind);
  */
 int qmc_wf_psi(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double* psi,
                void* scratch, int64_t scratch_bytes, void* stream);
+
+/*
+ * qmc_wf_psi_static: psi[w] exactly as qmc_wf_psi computes it, for callers
+ * that cannot allocate device memory on the call path -- for example a host
+ * application that hands its whole HBM budget to its own pool allocator (a
+ * cudaMalloc could fail or fragment that pool), a latency-critical loop in
+ * which cudaMalloc/cudaFree would implicitly synchronize the device, or a
+ * foreign-language binding that can pass device buffers but has no allocator
+ * hook. It has no counterpart in the reference.
+ *
+ * The caller passes positions and the output; the workspace is a fixed
+ * QMC_STATIC_SCRATCH_BYTES array compiled into this library (every GPU that
+ * loads the library keeps it for the life of the process). Limit: batches
+ * whose qmc_scratch_bytes(d, nwalkers, 0) exceeds QMC_STATIC_SCRATCH_BYTES are
+ * rejected with QMC_ERR_STATIC_LIMIT and nothing is launched (about 17,900
+ * walkers of H2O cc-pVDZ with single_double(4,4)). The library allocates
+ * nothing: no cudaMalloc, cudaFree or allocating library call.
+ *
+ * The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture. All calls share the one array and it keeps the
+ * previous call's contents; the kernel writes every element it reads, so
+ * nothing needs clearing between calls, but calls that overlap on the GPU
+ * (other streams, other host threads) race on it and must be serialized.
+ */
+#define QMC_STATIC_SCRATCH_BYTES (16 * 1024 * 1024)
+int qmc_wf_psi_static(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double* psi,
+                      void* stream);
 
 /*
  * eloc[w] = -1/2 lap(psi)/psi + V_en + V_ee + V_nn; kinetic[w] and psi[w] are

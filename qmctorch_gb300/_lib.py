@@ -116,6 +116,7 @@ SIGNATURES = {
     "qmc_metropolis_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
     "qmc_wf_psi": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                   c_void_p]),
+    "qmc_wf_psi_static": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_wf_local_energy": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                            c_void_p, c_void_p, c_int64, c_void_p]),
     "qmc_ao_eval": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_int32, c_void_p, c_void_p,

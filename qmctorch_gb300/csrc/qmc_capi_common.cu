@@ -18,6 +18,8 @@ const char* qmc_status_string(int s) {
     case QMC_ERR_SCRATCH: return "scratch buffer too small";
     case QMC_ERR_LAUNCH: return "CUDA launch error";
     case QMC_ERR_UNSUPPORTED: return "unsupported option";
+    case QMC_ERR_STATIC_LIMIT:
+      return "batch needs more scratch than the static array of qmc_wf_psi_static holds";
     default: return "unknown status";
   }
 }

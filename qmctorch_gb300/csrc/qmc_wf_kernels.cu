@@ -2,6 +2,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "qmc_host.cuh"
 
 namespace qmc {
@@ -90,3 +92,53 @@ int qmc_wf_local_energy(const qmc_wf_desc* d, const double* pos, int64_t nw, dou
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Static-scratch variant of qmc_wf_psi for callers that cannot allocate device
+// memory (see include/qmc_gb300.h). The workspace is this file-scope array;
+// host code may not use its name as a device address, so its address is looked
+// up once per device with cudaGetSymbolAddress and passed to the kernel.
+// ---------------------------------------------------------------------------
+static __device__ __align__(256) unsigned char g_psi_static_scratch[QMC_STATIC_SCRATCH_BYTES];
+
+namespace {
+constexpr int kMaxDevices = 64;
+std::mutex g_static_mutex;
+void* g_static_address[kMaxDevices] = {};
+
+// Device address of g_psi_static_scratch on the current device (looked up on
+// the first call per device, with that device current).
+int static_scratch_address(void** out) {
+  int dev = -1;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    cudaGetLastError();
+    return QMC_ERR_LAUNCH;
+  }
+  std::lock_guard<std::mutex> lock(g_static_mutex);
+  if (g_static_address[dev] == nullptr) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_psi_static_scratch);
+    if (e != cudaSuccess || p == nullptr) {
+      cudaGetLastError();
+      return QMC_ERR_LAUNCH;
+    }
+    g_static_address[dev] = p;
+  }
+  *out = g_static_address[dev];
+  return QMC_OK;
+}
+}  // namespace
+
+extern "C" int qmc_wf_psi_static(const qmc_wf_desc* d, const double* pos, int64_t nw,
+                                 double* psi, void* stream) {
+  int st = check_desc(d);
+  if (st) return st;
+  if (nw < 0 || (nw > 0 && (!pos || !psi))) return QMC_ERR_ARG;
+  if (nw == 0) return QMC_OK;
+  const int64_t need = qmc_scratch_bytes(d, nw, 0);
+  if (need < 0) return QMC_ERR_ARG;
+  if (need > (int64_t)QMC_STATIC_SCRATCH_BYTES) return QMC_ERR_STATIC_LIMIT;
+  void* scr = nullptr;
+  if ((st = static_scratch_address(&scr))) return st;
+  return qmc_wf_psi(d, pos, nw, psi, scr, need, stream);
+}
