@@ -46,6 +46,16 @@ enum qmc_status {
 #define QMC_DET_EXPLICIT 1   /* one LU per unique column set (det_explicit 96-111,
                                 operator_explicit 348-409) */
 
+/* Arithmetic of the fused kernels. QMC_PREC_FP64: the plain method, FP64
+   throughout. QMC_PREC_MIXED: AO values and derivatives, the AO->MO
+   contraction, the Jastrow factor and the Slater LU in FP32; electron-nucleus
+   and electron-electron differences formed in FP64 before rounding; spin
+   determinants, psi, local-energy sums and one iterative-refinement step of
+   the solves that feed the kinetic energy in FP64. The staged module kernels
+   (qmc_ao_eval, qmc_mo_eval, qmc_jastrow_ee, qmc_slater) are FP64 always. */
+#define QMC_PREC_FP64 0
+#define QMC_PREC_MIXED 1
+
 /*
  * Wave-function description. Built once per molecule by the host layer from
  * the basis namespace (AtomicOrbitals.__init__, atomic_orbitals.py:16-102),
@@ -69,6 +79,7 @@ typedef struct qmc_wf_desc {
   int32_t nweight;   /* AO-primitive weights (= basis entries) */
   int32_t contract;  /* 0 reproduces the uncontracted-basis value path (atomic_orbitals.py:246-249) */
   int32_t use_jastrow;
+  int32_t precision; /* QMC_PREC_FP64 or QMC_PREC_MIXED (fused psi / local energy / Metropolis) */
   /* basis tables */
   const double* atom_coords;  /* [natom*3] */
   const double* atom_charge;  /* [natom] */

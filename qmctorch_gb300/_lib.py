@@ -84,7 +84,7 @@ class WfDesc(ctypes.Structure):
         ("nelec", c_int32), ("nup", c_int32), ("ndown", c_int32), ("natom", c_int32),
         ("nao", c_int32), ("nmo", c_int32), ("nmo_used", c_int32), ("ngroup", c_int32),
         ("ngprim", c_int32), ("nweight", c_int32), ("contract", c_int32),
-        ("use_jastrow", c_int32),
+        ("use_jastrow", c_int32), ("precision", c_int32),
         ("atom_coords", c_void_p), ("atom_charge", c_void_p), ("group_atom", c_void_p),
         ("group_prim", c_void_p), ("group_ao", c_void_p), ("gprim_entry", c_void_p),
         ("bas_exp", c_void_p), ("ao_k", c_void_p), ("ao_wofs", c_void_p), ("ao_wd", c_void_p),

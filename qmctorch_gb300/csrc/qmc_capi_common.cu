@@ -26,12 +26,12 @@ const char* qmc_status_string(int s) {
 
 int64_t qmc_scratch_bytes(const qmc_wf_desc* d, int64_t nw, int32_t kind) {
   if (check_desc(d) != QMC_OK || nw < 0 || kind < 0 || kind > 1) return -1;
-  return scratch_items(d, kind) * pad_walkers(nw) * (int64_t)sizeof(double);
+  return scratch_slot_bytes(d, kind) * pad_walkers(nw);
 }
 
 int64_t qmc_metropolis_scratch_bytes(const qmc_wf_desc* d, int64_t nw) {
   if (check_desc(d) != QMC_OK || nw < 0) return -1;
-  return scratch_items(d, 2) * pad_walkers(nw) * (int64_t)sizeof(double);
+  return scratch_slot_bytes(d, 2) * pad_walkers(nw);
 }
 
 }  // extern "C"

@@ -1,0 +1,404 @@
+// Electron-parallel evaluation of psi / E_L for a block of walkers.
+//
+// A block owns `nwb` walkers and runs nwb * nelec threads: thread t handles
+// electron e = t / nwb of walker wl = t % nwb (with nwb = 32 one warp is one
+// electron of 32 walkers, so control flow is warp-uniform). Phases, separated
+// by block barriers that every thread reaches:
+//   1. electron phase (all threads): the electron's Jastrow row, its Coulomb
+//      terms and its MO row (plus the kinetic-operator row for E_L), written
+//      to shared memory;
+//   2. determinant phase (threads < 2 nwb): one thread per (walker, spin) runs
+//      the LU / excitation / trace work of spin_channel on the shared-memory MO
+//      rows, so both spins proceed in parallel;
+//   3. combine phase (threads < nwb): CI sum, Jastrow factor, energies.
+// Compared with one thread per walker this gives nelec times more threads
+// (about 34 warps per SM for 16384 H2O walkers) to hide FP32 and L1 latency.
+#pragma once
+
+#include "qmc_device.cuh"
+
+namespace qmc {
+
+// ---------------------------------------------------------------------------
+// shared-memory and scratch layouts
+// ---------------------------------------------------------------------------
+struct EPShape {
+  int nwb;       // walkers per block
+  int nthreads;  // threads per block
+  int64_t smem;  // dynamic shared memory bytes
+  int64_t o_tab, o_pos, o_pnew, o_mo, o_bk, o_jrow, o_vrow, o_dref, o_psi, o_f, o_kin, o_v,
+      o_iel, o_acc;
+};
+
+template <typename R>
+__host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb) {
+  EPShape s;
+  s.nwb = nwb;
+  int nt = nwb * d.nelec;
+  if (nt < 2 * nwb) nt = 2 * nwb;
+  s.nthreads = ((nt + 31) / 32) * 32;
+  const int64_t nc = 3 * (int64_t)d.nelec, nmu = d.nmo_used;
+  int64_t o = 0;
+  s.o_tab = o;
+  o += tables_smem_bytes<R>(d, d.nmo_used);
+  s.o_pos = o;
+  o += align8(nwb * nc * 8);
+  s.o_pnew = o;
+  if (kind == 2) o += align8(nwb * nc * 8);
+  s.o_mo = o;
+  o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
+  s.o_bk = o;
+  if (kind == 1) o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
+  s.o_jrow = o;
+  o += align8((int64_t)d.nelec * nwb * 8);
+  s.o_vrow = o;
+  if (kind == 1) o += align8((int64_t)d.nelec * nwb * 8);
+  s.o_dref = o;
+  o += 2 * nwb * 8;
+  s.o_psi = o;
+  o += nwb * 8;
+  s.o_f = o;
+  o += nwb * 8;
+  s.o_kin = o;
+  o += nwb * 8;
+  s.o_v = o;
+  o += nwb * 8;
+  s.o_iel = o;
+  o += align8(nwb * 4);
+  s.o_acc = o;
+  o += align8(nwb * 4);
+  s.smem = o;
+  return s;
+}
+
+// Thread bound of the electron-parallel kernels: 1024 threads (64 registers)
+// for FP32, 512 (128 registers) for FP64, whose accumulators are twice as wide.
+template <typename R>
+struct EPBound {
+  static constexpr int kThreads = kMixed<R> ? 1024 : 512;
+};
+
+// Largest walkers-per-block that fits the shared memory and the thread bound.
+template <typename R>
+__host__ inline EPShape ep_choose(const qmc_wf_desc& d, int kind) {
+  for (int nwb = 32; nwb > 1; nwb /= 2) {
+    const EPShape s = ep_shape<R>(d, kind, nwb);
+    if (s.nthreads <= EPBound<R>::kThreads && s.smem <= 200 * 1024) return s;
+  }
+  return ep_shape<R>(d, kind, 1);
+}
+
+// Per-walker scratch: the determinant-phase work arrays of both spins.
+struct EPLayout {
+  Region lu[2], x[2], y[2], x64[2], y64[2], rc[2], dv, ov;
+  int64_t bytes_per_slot;
+  int nmax, vmax, omax;
+};
+
+__host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
+  EPLayout L;
+  const bool mixed = d.precision == QMC_PREC_MIXED;
+  const int rsz = mixed ? 4 : 8;
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  int vmax = 0, omax = nmax;
+  if (d.det_mode == QMC_DET_EXCITATION) {
+    const int v0 = d.max_orb[0] - d.nup, v1 = d.max_orb[1] - d.ndown;
+    vmax = v0 > v1 ? v0 : v1;
+    omax = d.max_orb[0] > d.max_orb[1] ? d.max_orb[0] : d.max_orb[1];
+  }
+  L.nmax = nmax;
+  L.vmax = vmax;
+  L.omax = omax;
+  int64_t o = 0;
+  auto add = [&](Region& r, int64_t count, int esize) {
+    r.off = o;
+    r.esize = esize;
+    o += count * esize;
+  };
+  const bool el = kind == 1;
+  for (int s = 0; s < 2; ++s) {
+    add(L.lu[s], (int64_t)nmax * nmax, rsz);
+    add(L.x[s], (int64_t)nmax * vmax, rsz);
+    add(L.y[s], el ? (int64_t)nmax * omax : 0, rsz);
+    add(L.x64[s], (el && mixed) ? (int64_t)nmax * vmax : 0, 8);
+    add(L.y64[s], (el && mixed) ? (int64_t)nmax * omax : 0, 8);
+    add(L.rc[s], (el && mixed) ? nmax : 0, rsz);
+  }
+  add(L.dv, d.ndet[0] + d.ndet[1], 8);
+  add(L.ov, el ? d.ndet[0] + d.ndet[1] : 0, 8);
+  L.bytes_per_slot = align8(o);
+  return L;
+}
+
+// ---------------------------------------------------------------------------
+// AO groups, specialised by component count
+// ---------------------------------------------------------------------------
+// x^k and its first / second derivatives for the cartesian powers of s, p, d
+// shells by selects (no loop); larger powers fall back to ipow.
+template <typename R>
+__device__ __forceinline__ R pk0(R x, int k) {
+  return k == 0 ? (R)1 : (k == 1 ? x : (k == 2 ? x * x : ipow(x, k)));
+}
+template <typename R>
+__device__ __forceinline__ R pk1(R x, int k) {
+  return k == 0 ? (R)0 : (k == 1 ? (R)1 : (k == 2 ? (R)2 * x : (R)k * ipow(x, k - 1)));
+}
+template <typename R>
+__device__ __forceinline__ R pk2(R x, int k) {
+  return k < 2 ? (R)0 : (k == 2 ? (R)2 : (R)(k * (k - 1)) * ipow(x, k - 2));
+}
+
+template <typename R, bool DERIV, int NC, typename F>
+__device__ __forceinline__ void group_eval(const Tables<R>& t, int g, R dx, R dy, R dz, R r2,
+                                           F& f) {
+  const int p0 = t.group_prim[g], np = t.group_prim[g + 1] - p0;
+  const int a0 = t.group_ao[g];
+  const int wb = t.ao_wofs[a0];  // weights of component c at wb + c * np
+  R G0[NC], G1[NC], G2[NC];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) G0[c] = G1[c] = G2[c] = (R)0;
+  for (int p = 0; p < np; ++p) {
+    const R al = t.alpha[p0 + p];
+    const R e0 = rexp(-al * r2);
+    const R e1 = al * e0, e2 = al * e1;
+#pragma unroll
+    for (int c = 0; c < NC; ++c) {
+      const R w = t.wd[wb + c * np + p];
+      G0[c] = fma(w, e0, G0[c]);
+      if (DERIV) {
+        G1[c] = fma(w, e1, G1[c]);
+        G2[c] = fma(w, e2, G2[c]);
+      }
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const int a = a0 + c;
+    const int kx = t.ao_k[3 * a], ky = t.ao_k[3 * a + 1], kz = t.ao_k[3 * a + 2];
+    const R px = pk0(dx, kx), py = pk0(dy, ky), pz = pk0(dz, kz);
+    const R P = px * py * pz;
+    const R vs = t.vscale ? t.vscale[a] : (R)1;
+    AOVal<R> o;
+    o.v = vs * (P * G0[c]);
+    if (DERIV) {
+      const R qx = pk1(dx, kx), qy = pk1(dy, ky), qz = pk1(dz, kz);
+      const R lapP = pk2(dx, kx) * py * pz + px * pk2(dy, ky) * pz + px * py * pk2(dz, kz);
+      const R pg1 = (R)(-2) * P * G1[c];
+      o.gx = fma(qx * py * pz, G0[c], dx * pg1);
+      o.gy = fma(px * qy * pz, G0[c], dy * pg1);
+      o.gz = fma(px * py * qz, G0[c], dz * pg1);
+      const int l = kx + ky + kz;
+      o.lap = vs * fma(lapP, G0[c], P * ((R)4 * r2 * G2[c] - (R)(6 + 4 * l) * G1[c]));
+    }
+    f(a, o);
+  }
+}
+
+// All AOs of one electron; the electron-atom difference is formed once per
+// atom (groups are stored atom by atom).
+template <typename R, bool DERIV, typename F>
+__device__ __forceinline__ void for_each_ao_ep(const Tables<R>& t, double ex, double ey,
+                                               double ez, F&& f) {
+  int last = -1;
+  R dx = 0, dy = 0, dz = 0, r2 = 0;
+  for (int g = 0; g < t.ngroup; ++g) {
+    const int A = t.group_atom[g];
+    if (A != last) {
+      dx = (R)(ex - t.atom_xyz[3 * A]);
+      dy = (R)(ey - t.atom_xyz[3 * A + 1]);
+      dz = (R)(ez - t.atom_xyz[3 * A + 2]);
+      r2 = dx * dx + dy * dy + dz * dz;
+      last = A;
+    }
+    switch (t.group_ao[g + 1] - t.group_ao[g]) {
+      case 1: group_eval<R, DERIV, 1>(t, g, dx, dy, dz, r2, f); break;
+      case 2: group_eval<R, DERIV, 2>(t, g, dx, dy, dz, r2, f); break;
+      case 3: group_eval<R, DERIV, 3>(t, g, dx, dy, dz, r2, f); break;
+      case 4: group_eval<R, DERIV, 4>(t, g, dx, dy, dz, r2, f); break;
+      case 5: group_eval<R, DERIV, 5>(t, g, dx, dy, dz, r2, f); break;
+      default: group_eval<R, DERIV, 6>(t, g, dx, dy, dz, r2, f); break;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// phase 1: one electron of one walker
+// ---------------------------------------------------------------------------
+// pw: the walker's positions (shared memory, FP64). mo / bk: element (e, j) of
+// this walker at [(e * nmu + j) * nwb]. jrow: log J partial of this electron;
+// vrow (E_L): its V_en plus half its V_ee row.
+template <typename R, int JC, bool KIN>
+__device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, const double* pw,
+                                   int e, R* mo, R* bk, int nwb, double* jrow, double* vrow) {
+  const int ne = d.nelec, nmu = d.nmo_used;
+  const double ex = pw[3 * e], ey = pw[3 * e + 1], ez = pw[3 * e + 2];
+  R gx = (R)0, gy = (R)0, gz = (R)0, jl = (R)0;
+  {
+    const R w = (R)__ldg(d.jastrow_w);
+    R ks = (R)0, vs = (R)0, lp = (R)0;
+    if (d.use_jastrow || KIN) {
+      for (int j = KIN ? 0 : e + 1; j < ne; ++j) {
+        if (j == e) continue;
+        const R dx = (R)(ex - pw[3 * j]), dy = (R)(ey - pw[3 * j + 1]), dz = (R)(ez - pw[3 * j + 2]);
+        const R r = rsqrt_(dx * dx + dy * dy + dz * dz);
+        if (KIN) vs += (R)1 / r;
+        if (d.use_jastrow) {
+          const R w0 = same_spin(d, e, j) ? (R)0.25 : (R)0.5;
+          const R iu = (R)1 / ((R)1 + w * r);
+          ks += w0 * r * iu;
+          if (KIN) {
+            const R ir = (R)1 / r;
+            const R k1 = w0 * iu * iu;                       // dK/dr
+            gx += k1 * dx * ir;
+            gy += k1 * dy * ir;
+            gz += k1 * dz * ir;
+            lp += (R)2 * k1 * ir - (R)2 * w * k1 * iu;        // 2K'/r + K''
+          }
+        }
+      }
+    }
+    if (KIN) {
+      jl = lp + gx * gx + gy * gy + gz * gz;  // lap(J)/J of this electron
+      *jrow = 0.5 * (double)ks;               // every pair visited from both ends
+      R ven = (R)0;
+      for (int A = 0; A < t.natom; ++A) {
+        const R dx = (R)(ex - t.atom_xyz[3 * A]), dy = (R)(ey - t.atom_xyz[3 * A + 1]),
+                dz = (R)(ez - t.atom_xyz[3 * A + 2]);
+        ven -= (R)t.atom_z[A] / rsqrt_(dx * dx + dy * dy + dz * dz);
+      }
+      *vrow = 0.5 * (double)vs + (double)ven;
+    } else {
+      *jrow = (double)ks;
+    }
+  }
+  const int64_t cs = nwb;
+  R* mrow = mo + (int64_t)e * nmu * cs;
+  R* brow = KIN ? bk + (int64_t)e * nmu * cs : nullptr;
+  for (int j0 = 0; j0 < nmu; j0 += JC) {
+    R a0[JC], ad[JC], al[JC];
+#pragma unroll
+    for (int jj = 0; jj < JC; ++jj) a0[jj] = ad[jj] = al[jj] = (R)0;
+    auto acc = [&](int a, const AOVal<R>& o) {
+      const R* Wa = t.W + (int64_t)a * t.ncol + j0;
+      R gdot = (R)0;
+      if (KIN) gdot = (R)2 * (gx * o.gx + gy * o.gy + gz * o.gz);
+#pragma unroll
+      for (int jj = 0; jj < JC; ++jj) {
+        if (j0 + jj < nmu) {
+          const R wj = Wa[jj];
+          a0[jj] = fma(o.v, wj, a0[jj]);
+          if (KIN) {
+            ad[jj] = fma(gdot, wj, ad[jj]);
+            al[jj] = fma(o.lap, wj, al[jj]);
+          }
+        }
+      }
+    };
+    for_each_ao_ep<R, KIN>(t, ex, ey, ez, acc);
+#pragma unroll
+    for (int jj = 0; jj < JC; ++jj) {
+      if (j0 + jj < nmu) {
+        mrow[(j0 + jj) * cs] = a0[jj];
+        if (KIN) brow[(j0 + jj) * cs] = (R)(-0.5) * (al[jj] + ad[jj] + jl * a0[jj]);
+      }
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// phases 2 and 3
+// ---------------------------------------------------------------------------
+template <typename R, bool OP>
+__device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned char* scr,
+                              int64_t ss, int64_t w, int spin, const R* mo_s, const R* bk_s, int wl,
+                              int nwb, double* dref) {
+  const int row0 = spin ? d.nup : 0;
+  const int64_t cs = nwb, rs = (int64_t)d.nmo_used * nwb;
+  const CView<R> mo{mo_s + row0 * rs + wl, rs, cs};
+  const CView<R> bk{(OP ? bk_s : mo_s) + row0 * rs + wl, rs, cs};
+  const int64_t vm = L.vmax > 0 ? L.vmax : 1;
+  SpinWork<R> wk;
+  wk.LU = MView<R>{rptr<R>(scr, L.lu[spin], ss, w), (int64_t)L.nmax * ss, ss};
+  wk.X = MView<R>{rptr<R>(scr, L.x[spin], ss, w), vm * ss, ss};
+  wk.Y = MView<R>{rptr<R>(scr, L.y[spin], ss, w), (int64_t)L.omax * ss, ss};
+  wk.rc = MView<R>{rptr<R>(scr, L.rc[spin], ss, w), ss, ss};
+  wk.X64 = MView<double>{rptr<double>(scr, L.x64[spin], ss, w), vm * ss, ss};
+  wk.Y64 = MView<double>{rptr<double>(scr, L.y64[spin], ss, w), (int64_t)L.omax * ss, ss};
+  double* dv = rptr<double>(scr, L.dv, ss, w) + (spin ? d.ndet[0] * ss : 0);
+  double* ov = OP ? rptr<double>(scr, L.ov, ss, w) + (spin ? d.ndet[0] * ss : 0) : nullptr;
+  spin_channel<R, OP>(d, spin, mo, bk, wk, SpinOut{dv, ov, ss, &dref[spin * nwb + wl]});
+}
+
+struct EPPtrs {
+  unsigned char* smem;
+  EPShape S;
+};
+
+// Evaluate psi (and, with KIN, the kinetic energy and potentials) for the
+// block's walkers at positions `pbuf` (shared memory, [nwb][3 nelec]).
+// Results in shared memory: psi[wl], and with KIN kin[wl], v[wl] (V_en + V_ee).
+// Every thread of the block must call this (it contains block barriers).
+template <typename R, int JC, bool KIN>
+__device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const EPPtrs& p,
+                               const double* pbuf, unsigned char* scr, int64_t ss, int64_t w0,
+                               int64_t nw) {
+  const EPShape& S = p.S;
+  const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne;
+  const int tid = threadIdx.x;
+  R* MO = reinterpret_cast<R*>(p.smem + S.o_mo);
+  R* BK = reinterpret_cast<R*>(p.smem + S.o_bk);
+  double* JR = reinterpret_cast<double*>(p.smem + S.o_jrow);
+  double* VR = reinterpret_cast<double*>(p.smem + S.o_vrow);
+  double* DREF = reinterpret_cast<double*>(p.smem + S.o_dref);
+  double* PSI = reinterpret_cast<double*>(p.smem + S.o_psi);
+  double* KINV = reinterpret_cast<double*>(p.smem + S.o_kin);
+  double* V = reinterpret_cast<double*>(p.smem + S.o_v);
+  {
+    const int e = tid / nwb, wl = tid - (tid / nwb) * nwb;
+    if (e < ne)
+      ep_electron<R, JC, KIN>(d, t, pbuf + wl * nc, e, MO + wl, BK + wl, nwb, &JR[e * nwb + wl],
+                              &VR[e * nwb + wl]);
+  }
+  __syncthreads();
+  const EPLayout L = ep_layout(d, KIN ? 1 : 0);
+  if (tid < 2 * nwb) {
+    const int spin = tid / nwb, wl = tid - spin * nwb;
+    if (w0 + wl < nw) ep_det<R, KIN>(d, L, scr, ss, w0 + wl, spin, MO, BK, wl, nwb, DREF);
+  }
+  __syncthreads();
+  if (tid < nwb && w0 + tid < nw) {
+    const int wl = tid;
+    const int64_t w = w0 + wl;
+    double kin = 0.0;
+    const double* dv = rptr<double>(scr, L.dv, ss, w);
+    const double* ov = KIN ? rptr<double>(scr, L.ov, ss, w) : nullptr;
+    using A = typename std::conditional<KIN, double, R>::type;
+    const double psid = ci_combine<A, KIN>(d, dv, ov, ss, DREF[wl], DREF[nwb + wl], &kin);
+    double logj = 0.0, v = 0.0;
+    for (int e = 0; e < ne; ++e) {
+      logj += JR[e * nwb + wl];
+      if (KIN) v += VR[e * nwb + wl];
+    }
+    PSI[wl] = d.use_jastrow ? psid * exp(logj) : psid;
+    if (KIN) {
+      KINV[wl] = kin;
+      V[wl] = v;
+    }
+  }
+  __syncthreads();
+}
+
+// Stage the positions of walkers [w0, w0 + nwb) into shared memory; slots past
+// the last walker repeat walker nw - 1 (a valid configuration, never stored).
+__device__ inline void ep_stage_positions(const double* pos, int64_t w0, int64_t nw, int nwb,
+                                          int nc, double* P) {
+  for (int i = threadIdx.x; i < nwb * nc; i += blockDim.x) {
+    const int wl = i / nc, c = i - wl * nc;
+    int64_t w = w0 + wl;
+    if (w >= nw) w = nw - 1;
+    P[i] = pos[w * nc + c];
+  }
+  __syncthreads();
+}
+
+}  // namespace qmc

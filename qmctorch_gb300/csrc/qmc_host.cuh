@@ -5,10 +5,11 @@
 #include <stdint.h>
 
 #include "qmc_device.cuh"
+#include "qmc_ep.cuh"
 
 namespace qmc {
 
-constexpr int kTPB = 64;  // threads (= walkers) per block
+constexpr int kTPB = 32;  // threads (= walkers) per block: one warp, for balance over 152 SMs
 
 __host__ __device__ inline int64_t pad_walkers(int64_t nw) { return (nw + 31) & ~int64_t(31); }
 
@@ -27,6 +28,7 @@ static inline int check_desc(const qmc_wf_desc* d) {
   if (d->use_jastrow && !d->jastrow_w) return QMC_ERR_ARG;
   if (d->nmo_used > d->nmo || d->nmo_used < 1) return QMC_ERR_ARG;
   if (d->det_mode != QMC_DET_EXCITATION && d->det_mode != QMC_DET_EXPLICIT) return QMC_ERR_ARG;
+  if (d->precision != QMC_PREC_FP64 && d->precision != QMC_PREC_MIXED) return QMC_ERR_ARG;
   return QMC_OK;
 }
 
@@ -46,6 +48,18 @@ static inline int prepare_smem(K kernel, int64_t bytes) {
   return QMC_OK;
 }
 
-static inline int64_t scratch_items(const qmc_wf_desc* d, int kind) { return scratch_layout(*d, kind).total; }
+// Per-walker scratch bytes: the fused kernels use the electron-parallel
+// layout (kinds 0 psi, 1 local energy, 2 Metropolis); kind 1 also covers the
+// staged pooling kernel (one thread per walker, FP64).
+static inline int64_t scratch_slot_bytes(const qmc_wf_desc* d, int kind) {
+  int64_t b = ep_layout(*d, kind == 2 ? 0 : kind).bytes_per_slot;
+  if (kind == 1) {
+    qmc_wf_desc dd = *d;
+    dd.precision = QMC_PREC_FP64;
+    const int64_t t = scratch_layout(dd, 1).bytes_per_slot;
+    if (t > b) b = t;
+  }
+  return b;
+}
 
 }  // namespace qmc

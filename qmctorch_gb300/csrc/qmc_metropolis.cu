@@ -2,6 +2,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "qmc_ep.cuh"
 #include "qmc_host.cuh"
 
 namespace qmc {
@@ -50,116 +51,168 @@ struct Rng {
   }
 };
 
-template <int JC>
-__global__ void __launch_bounds__(kTPB) metropolis_kernel(const qmc_wf_desc d, const qmc_metropolis_args a,
-                                                          double* __restrict__ scr, int64_t ss) {
+// One block advances `nwb` walker chains through all steps. Per move: every
+// electron thread writes its proposed coordinates (Philox normals or the
+// replay input), the block evaluates psi at the proposal (qmc_ep.cuh), the
+// walker's combine thread takes the accept decision, and the electron threads
+// copy accepted coordinates. Generator: counter (call, walker, step), key
+// (seed); call = move * (nelec + 2) + e for electron e's three normals,
+// + nelec for the accept uniform, + nelec + 1 for the one-elec electron index.
+template <typename R, int JC>
+__global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const qmc_wf_desc d, const qmc_metropolis_args a,
+                                                          unsigned char* __restrict__ scr, int64_t ss,
+                                                          const EPShape S) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables t = load_tables(d, d.nmo_used, smem);
-  const Layout L = scratch_layout(d, 2);
+  const Tables<R> t = load_tables<R>(d, d.nmo_used, smem + S.o_tab);
   const int64_t nw = a.nwalkers;
-  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= nw) return;
-  const int ne = d.nelec, nc = 3 * ne;
-  double* sw = scr + w;
-  double* xp = sw + L.pos * ss;   // current positions
-  double* xn = sw + L.pnew * ss;  // proposal
-  for (int c = 0; c < nc; ++c) xp[c * ss] = a.pos[w * nc + c];
-  const PosView Pc{xp, ss}, Pn{xn, ss};
+  const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne;
+  const int64_t w0 = (int64_t)blockIdx.x * nwb;
+  const int tid = threadIdx.x;
+  const int e = tid / nwb, wl = tid - (tid / nwb) * nwb;
+  const int64_t w = w0 + wl;
+  const bool live = e < ne && w < nw;  // electron thread of a real walker
+  double* P = reinterpret_cast<double*>(smem + S.o_pos);    // current positions
+  double* PN = reinterpret_cast<double*>(smem + S.o_pnew);  // proposal
+  double* PSI = reinterpret_cast<double*>(smem + S.o_psi);
+  double* F = reinterpret_cast<double*>(smem + S.o_f);
+  int* IEL = reinterpret_cast<int*>(smem + S.o_iel);
+  int* ACC = reinterpret_cast<int*>(smem + S.o_acc);
+  const EPPtrs ptrs{smem, S};
   const double eps = 1e-16;
-  double psi = walker_psi<JC>(d, t, L, Pc, sw, ss);
-  double fx = psi * psi;
-  if (fx == 0.0) fx = eps;
+  ep_stage_positions(a.pos, w0, nw, nwb, nc, P);
+  ep_eval<R, JC, false>(d, t, ptrs, P, scr, ss, w0, nw);
+  int nacc = 0;
+  double psi_cur = 0.0;  // combine threads: psi at the current positions
+  if (tid < nwb) {
+    psi_cur = PSI[tid];
+    const double f = psi_cur * psi_cur;
+    F[tid] = f == 0.0 ? eps : f;
+  }
   const double sigma = a.step_size / (2.0 * sqrt(2.0 * log(2.0)));
   const double sd = sqrt(sigma);  // MultivariateNormal(0, sigma I): std = sqrt(sigma)
   Rng rng{(uint32_t)a.seed, (uint32_t)(a.seed >> 32), (uint32_t)w, 0, 0};
   const int nmove = a.move_type == QMC_MOVE_ALL_ELEC_ITER ? ne : 1;
-  int nacc = 0;
   int64_t isnap = 0, idecor = 0;
   for (int istep = 0; istep < a.nstep; ++istep) {
     rng.step = a.step_offset + istep;
-    rng.call = 0;
     for (int im = 0; im < nmove; ++im) {
-      double u;
-      if (a.move_type == QMC_MOVE_ALL_ELEC) {
-        if (a.proposals) {
-          const double* pr = a.proposals + ((int64_t)istep * nw + w) * nc;
-          for (int c = 0; c < nc; ++c) xn[c * ss] = xp[c * ss] + pr[c];
-          u = a.uniforms[(int64_t)istep * nw + w];
-        } else {
-          for (int c = 0; c < nc; c += 4) {
-            const U4 r = rng.next();
-            double z[4];
-            if (a.proba == QMC_PROBA_NORMAL) {
-              rng.normal2(r.x, r.y, z[0], z[1]);
-              rng.normal2(r.z, r.w, z[2], z[3]);
-#pragma unroll
-              for (int q = 0; q < 4; ++q) z[q] *= sd;
+      const uint32_t call0 = (uint32_t)im * (uint32_t)(ne + 2);
+      // which electron moves
+      if (a.move_type == QMC_MOVE_ONE_ELEC) {
+        if (tid < nwb) {
+          int iel = 0;
+          if (w0 + tid < nw) {
+            if (a.proposals) {
+              iel = a.electron_index[(int64_t)istep * nw + w0 + tid];
             } else {
-              const uint32_t rr[4] = {r.x, r.y, r.z, r.w};
-#pragma unroll
-              for (int q = 0; q < 4; ++q) z[q] = a.step_size * (2.0 * (rr[q] * 2.3283064365386963e-10) - 1.0);
+              rng.call = call0 + ne + 1;
+              const U4 r = rng.next();
+              iel = (int)(((uint64_t)r.x * (uint64_t)ne) >> 32);
             }
-#pragma unroll
-            for (int q = 0; q < 4; ++q)
-              if (c + q < nc) xn[(c + q) * ss] = xp[(c + q) * ss] + z[q];
           }
+          IEL[tid] = iel;
+        }
+        __syncthreads();
+      }
+      // proposal
+      if (live) {
+        const bool moves = a.move_type == QMC_MOVE_ALL_ELEC ||
+                           (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]);
+        double z[3] = {0.0, 0.0, 0.0};
+        if (moves) {
+          if (a.proposals) {
+            if (a.move_type == QMC_MOVE_ALL_ELEC) {
+              const double* pr = a.proposals + ((int64_t)istep * nw + w) * nc + 3 * e;
+              z[0] = pr[0];
+              z[1] = pr[1];
+              z[2] = pr[2];
+            } else {
+              const double* pr = a.proposals + (((int64_t)istep * nmove + im) * nw + w) * 3;
+              z[0] = pr[0];
+              z[1] = pr[1];
+              z[2] = pr[2];
+            }
+          } else {
+            rng.call = call0 + e;
+            const U4 r = rng.next();
+            if (a.proba == QMC_PROBA_NORMAL) {
+              double z3;
+              rng.normal2(r.x, r.y, z[0], z[1]);
+              rng.normal2(r.z, r.w, z[2], z3);
+              z[0] *= sd;
+              z[1] *= sd;
+              z[2] *= sd;
+            } else {
+              const uint32_t rr[3] = {r.x, r.y, r.z};
+              for (int q = 0; q < 3; ++q)
+                z[q] = a.step_size * (2.0 * (rr[q] * 2.3283064365386963e-10) - 1.0);
+            }
+          }
+        }
+        for (int q = 0; q < 3; ++q) PN[wl * nc + 3 * e + q] = P[wl * nc + 3 * e + q] + z[q];
+      } else if (e < ne) {
+        for (int q = 0; q < 3; ++q) PN[wl * nc + 3 * e + q] = P[wl * nc + 3 * e + q];
+      }
+      __syncthreads();
+      ep_eval<R, JC, false>(d, t, ptrs, PN, scr, ss, w0, nw);
+      // accept / reject (metropolis.py:141-160, 279-298)
+      if (tid < nwb && w0 + tid < nw) {
+        double u;
+        if (a.proposals) {
+          u = a.move_type == QMC_MOVE_ALL_ELEC
+                  ? a.uniforms[(int64_t)istep * nw + w0 + tid]
+                  : a.uniforms[((int64_t)istep * nmove + im) * nw + w0 + tid];
+        } else {
+          rng.call = call0 + ne;
           const U4 r = rng.next();
           u = rng.uniform53(r.x, r.y);
         }
-      } else {
-        int iel;
-        double dz[3];
-        if (a.proposals) {
-          const int64_t mi = ((int64_t)istep * nmove + im) * nw + w;
-          iel = a.move_type == QMC_MOVE_ALL_ELEC_ITER ? im : a.electron_index[(int64_t)istep * nw + w];
-          for (int q = 0; q < 3; ++q) dz[q] = a.proposals[mi * 3 + q];
-          u = a.uniforms[mi];
-        } else {
-          const U4 r = rng.next();
-          const U4 r2 = rng.next();
-          if (a.proba == QMC_PROBA_NORMAL) {
-            double z3;
-            rng.normal2(r.x, r.y, dz[0], dz[1]);
-            rng.normal2(r.z, r.w, dz[2], z3);
-            for (int q = 0; q < 3; ++q) dz[q] *= sd;
-          } else {
-            const uint32_t rr[3] = {r.x, r.y, r.z};
-            for (int q = 0; q < 3; ++q) dz[q] = a.step_size * (2.0 * (rr[q] * 2.3283064365386963e-10) - 1.0);
-          }
-          u = rng.uniform53(r2.x, r2.y);
-          iel = a.move_type == QMC_MOVE_ALL_ELEC_ITER
-                    ? im
-                    : (int)(((uint64_t)r2.z * (uint64_t)ne) >> 32);
+        double fxn = PSI[tid] * PSI[tid];
+        if (fxn == 0.0) fxn = eps;
+        double df = fxn / F[tid];
+        if (df > 1.0) df = 1.0;
+        const int acc = (df - u >= 0.0) ? 1 : 0;
+        ACC[tid] = acc;
+        if (acc) {
+          F[tid] = fxn;
+          psi_cur = PSI[tid];
+          ++nacc;
         }
-        for (int c = 0; c < nc; ++c) xn[c * ss] = xp[c * ss];
-        for (int q = 0; q < 3; ++q) xn[(3 * iel + q) * ss] += dz[q];
       }
-      const double psin = walker_psi<JC>(d, t, L, Pn, sw, ss);
-      double fxn = psin * psin;
-      if (fxn == 0.0) fxn = eps;
-      double df = fxn / fx;
-      if (df > 1.0) df = 1.0;
-      if (df - u >= 0.0) {
-        for (int c = 0; c < nc; ++c) xp[c * ss] = xn[c * ss];
-        fx = fxn;
-        psi = psin;
-        ++nacc;
-      }
+      __syncthreads();
+      if (live && ACC[wl])
+        for (int q = 0; q < 3; ++q) P[wl * nc + 3 * e + q] = PN[wl * nc + 3 * e + q];
+      __syncthreads();
     }
     if (istep >= a.ntherm) {
       if (idecor % a.ndecor == 0) {
-        if (a.samples && isnap < a.nsnap) {
-          double* out = a.samples + (isnap * nw + w) * nc;
-          for (int c = 0; c < nc; ++c) out[c] = xp[c * ss];
+        if (a.samples && isnap < a.nsnap && live) {
+          double* out = a.samples + (isnap * nw + w) * nc + 3 * e;
+          for (int q = 0; q < 3; ++q) out[q] = P[wl * nc + 3 * e + q];
         }
         ++isnap;
       }
       ++idecor;
     }
   }
-  for (int c = 0; c < nc; ++c) a.pos[w * nc + c] = xp[c * ss];
-  if (a.accepted) a.accepted[w] += nacc;
-  if (a.psi_out) a.psi_out[w] = psi;
+  if (live)
+    for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = P[wl * nc + 3 * e + q];
+  if (tid < nwb && w0 + tid < nw) {
+    if (a.accepted) a.accepted[w0 + tid] += nacc;
+    if (a.psi_out) a.psi_out[w0 + tid] = psi_cur;
+  }
+}
+
+template <typename R, int JC>
+static int launch_metropolis(const qmc_wf_desc* d, const qmc_metropolis_args* a, unsigned char* scr,
+                             cudaStream_t s) {
+  const EPShape S = ep_choose<R>(*d, 2);
+  if (S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
+  int st = prepare_smem(metropolis_kernel<R, JC>, S.smem);
+  if (st) return st;
+  const dim3 grid((unsigned)((a->nwalkers + S.nwb - 1) / S.nwb));
+  metropolis_kernel<R, JC><<<grid, S.nthreads, S.smem, s>>>(*d, *a, scr, pad_walkers(a->nwalkers), S);
+  return launch_status();
 }
 
 }  // namespace qmc
@@ -180,22 +233,16 @@ int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void*
   if (a->proposals && !a->uniforms) return QMC_ERR_ARG;
   if (a->proposals && a->move_type == QMC_MOVE_ONE_ELEC && !a->electron_index) return QMC_ERR_ARG;
   if (scratch_bytes < qmc_metropolis_scratch_bytes(d, a->nwalkers)) return QMC_ERR_SCRATCH;
-  const int64_t smem = tables_smem_bytes(*d, d->nmo_used);
-  const int64_t ss = pad_walkers(a->nwalkers);
-  const dim3 grid((unsigned)((a->nwalkers + kTPB - 1) / kTPB));
   cudaStream_t s = (cudaStream_t)stream;
-  double* scr = (double*)scratch;
-  if (d->nmo_used <= 8) {
-    if ((st = prepare_smem(metropolis_kernel<8>, smem))) return st;
-    metropolis_kernel<8><<<grid, kTPB, smem, s>>>(*d, *a, scr, ss);
-  } else if (d->nmo_used <= 16) {
-    if ((st = prepare_smem(metropolis_kernel<16>, smem))) return st;
-    metropolis_kernel<16><<<grid, kTPB, smem, s>>>(*d, *a, scr, ss);
-  } else {
-    if ((st = prepare_smem(metropolis_kernel<24>, smem))) return st;
-    metropolis_kernel<24><<<grid, kTPB, smem, s>>>(*d, *a, scr, ss);
+  unsigned char* scr = (unsigned char*)scratch;
+  if (d->precision == QMC_PREC_MIXED) {
+    if (d->nmo_used <= 8) return launch_metropolis<float, 8>(d, a, scr, s);
+    if (d->nmo_used <= 16) return launch_metropolis<float, 16>(d, a, scr, s);
+    return launch_metropolis<float, 24>(d, a, scr, s);
   }
-  return launch_status();
+  if (d->nmo_used <= 8) return launch_metropolis<double, 8>(d, a, scr, s);
+  if (d->nmo_used <= 16) return launch_metropolis<double, 16>(d, a, scr, s);
+  return launch_metropolis<double, 24>(d, a, scr, s);
 }
 
 }  // extern "C"

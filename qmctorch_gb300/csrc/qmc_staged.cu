@@ -13,16 +13,16 @@ __global__ void __launch_bounds__(128) ao_kernel(const qmc_wf_desc d, const doub
                                                  int64_t nw, int mode, double* __restrict__ ao,
                                                  double* __restrict__ dao, double* __restrict__ d2ao) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables t = load_tables(d, 0, smem);
+  const Tables<double> t = load_tables<double>(d, 0, smem);
   const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // (walker, electron)
   if (item >= nw * d.nelec) return;
   const double* pe = pos + item * 3;  // pos[w][3*ne] row-major == [(w*ne+e)*3]
   const double ex = pe[0], ey = pe[1], ez = pe[2];
   const int64_t row = item * d.nao;
   if (mode == 0) {
-    for_each_ao<false>(t, ex, ey, ez, [&](int a, const AOVal& o) { ao[row + a] = o.v; });
+    for_each_ao<double, false>(t, ex, ey, ez, [&](int a, const AOVal<double>& o) { ao[row + a] = o.v; });
   } else {
-    for_each_ao<true>(t, ex, ey, ez, [&](int a, const AOVal& o) {
+    for_each_ao<double, true>(t, ex, ey, ez, [&](int a, const AOVal<double>& o) {
       if (mode == 1 || mode == 4) {
         dao[(row + a) * 3] = o.gx;
         dao[(row + a) * 3 + 1] = o.gy;
@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(128) ao_kernel(const qmc_wf_desc d, const doub
 __global__ void __launch_bounds__(128) mo_kernel(const qmc_wf_desc d, const double* __restrict__ ao,
                                                  int64_t nrows, double* __restrict__ mo) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables t = load_tables(d, d.nmo, smem);
+  const Tables<double> t = load_tables<double>(d, d.nmo, smem);
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
   const double* ar = ao + r * d.nao;
@@ -76,7 +76,7 @@ __global__ void __launch_bounds__(128) jastrow_kernel(const qmc_wf_desc d, const
   const int ne = d.nelec;
   PosView P{pos + w * 3 * ne, 1};
   const double wj = __ldg(d.jastrow_w);
-  const double J = exp(jastrow_log(d, P, wj));
+  const double J = exp(jastrow_log<double>(d, P, wj));
   if (jast) jast[w] = J;
   if (!djast && !d2jast) return;
   for (int i = 0; i < ne; ++i) {
@@ -88,7 +88,7 @@ __global__ void __launch_bounds__(128) jastrow_kernel(const qmc_wf_desc d, const
       const double r = sqrt(dx * dx + dy * dy + dz * dz);
       const double ir = 1.0 / r;
       const double iu = 1.0 / (1.0 + wj * r);
-      const double k1 = pade_w0(d, i, j) * iu * iu;
+      const double k1 = (same_spin(d, i, j) ? 0.25 : 0.5) * iu * iu;
       gx += k1 * dx * ir;
       gy += k1 * dy * ir;
       gz += k1 * dz * ir;
@@ -112,25 +112,24 @@ __global__ void __launch_bounds__(kTPB) slater_kernel(const qmc_wf_desc d, const
                                                       const double* __restrict__ bop, int ld,
                                                       int64_t nw, double* __restrict__ dets,
                                                       double* __restrict__ op,
-                                                      double* __restrict__ scr, int64_t ss) {
+                                                      unsigned char* __restrict__ scr, int64_t ss) {
   const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (w >= nw) return;
-  const Layout L = scratch_layout(d, 1);
-  double* sw = scr + w;
+  const Layout L = scratch_layout(d, 1);  // d.precision is QMC_PREC_FP64 here
   const int ne = d.nelec;
-  CView m{mo + w * ne * ld, ld, 1};
-  CView b = OP ? CView{bop + w * ne * ld, ld, 1} : m;
-  MView LU{sw + L.lu * ss, (int64_t)L.nmax * ss, ss};
-  MView X{sw + L.x * ss, (int64_t)(L.vmax > 0 ? L.vmax : 1) * ss, ss};
-  MView Y{sw + L.y * ss, (int64_t)L.omax * ss, ss};
-  double* dv = sw + L.dv * ss;
-  double* ov = sw + L.ov * ss;
-  spin_channel<OP>(d, 0, m, b, LU, X, Y, SpinOut{dv, ov, ss});
-  spin_channel<OP>(d, 1, CView{m.p + d.nup * m.rs, m.rs, m.cs}, CView{b.p + d.nup * b.rs, b.rs, b.cs},
-                   LU, X, Y, SpinOut{dv + d.ndet[0] * ss, ov + d.ndet[0] * ss, ss});
+  const CView<double> m{mo + w * ne * ld, ld, 1};
+  const CView<double> b = OP ? CView<double>{bop + w * ne * ld, ld, 1} : m;
+  const SpinWork<double> wk = spin_work<double>(L, scr, ss, w);
+  double* dv = rptr<double>(scr, L.dv, ss, w);
+  double* ov = rptr<double>(scr, L.ov, ss, w);
+  double dref[2];
+  spin_channel<double, OP>(d, 0, m, b, wk, SpinOut{dv, ov, ss, &dref[0]});
+  spin_channel<double, OP>(d, 1, CView<double>{m.p + d.nup * m.rs, m.rs, m.cs},
+                           CView<double>{b.p + d.nup * b.rs, b.rs, b.cs}, wk,
+                           SpinOut{dv + d.ndet[0] * ss, ov + d.ndet[0] * ss, ss, &dref[1]});
   for (int k = 0; k < d.ncfg; ++k) {
     const int iu = __ldg(d.cfg_det[0] + k), idn = __ldg(d.cfg_det[1] + k) + d.ndet[0];
-    dets[w * d.ncfg + k] = dv[iu * ss] * dv[idn * ss];
+    dets[w * d.ncfg + k] = (dref[0] * dv[iu * ss]) * (dref[1] * dv[idn * ss]);
     if (OP) op[w * d.ncfg + k] = ov[iu * ss] + ov[idn * ss];
   }
 }
@@ -180,7 +179,7 @@ int qmc_ao_eval(const qmc_wf_desc* d, const double* pos, int64_t nw, int32_t mod
   if ((mode == 1 || mode == 4) && !dao) return QMC_ERR_ARG;
   if ((mode == 2 || mode == 4) && !d2ao) return QMC_ERR_ARG;
   if (nw == 0) return QMC_OK;
-  const int64_t smem = tables_smem_bytes(*d, 0);
+  const int64_t smem = tables_smem_bytes<double>(*d, 0);
   if ((st = prepare_smem(ao_kernel, smem))) return st;
   const int64_t items = nw * d->nelec;
   ao_kernel<<<(unsigned)((items + 127) / 128), 128, smem, (cudaStream_t)stream>>>(*d, pos, nw, mode,
@@ -193,7 +192,7 @@ int qmc_mo_eval(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* m
   if (st) return st;
   if (nrows < 0 || (nrows > 0 && (!ao || !mo))) return QMC_ERR_ARG;
   if (nrows == 0) return QMC_OK;
-  const int64_t smem = tables_smem_bytes(*d, d->nmo);
+  const int64_t smem = tables_smem_bytes<double>(*d, d->nmo);
   if ((st = prepare_smem(mo_kernel, smem))) return st;
   mo_kernel<<<(unsigned)((nrows + 127) / 128), 128, smem, (cudaStream_t)stream>>>(*d, ao, nrows, mo);
   return launch_status();
@@ -211,22 +210,26 @@ int qmc_jastrow_ee(const qmc_wf_desc* d, const double* pos, int64_t nw, double* 
   return launch_status();
 }
 
-int qmc_slater(const qmc_wf_desc* d, const double* mo, const double* bop, int32_t ld, int64_t nw,
+int qmc_slater(const qmc_wf_desc* d0, const double* mo, const double* bop, int32_t ld, int64_t nw,
                double* dets, double* op, void* scratch, int64_t scratch_bytes, void* stream) {
-  int st = check_desc(d);
+  int st = check_desc(d0);
   if (st) return st;
+  qmc_wf_desc dd = *d0;
+  dd.precision = QMC_PREC_FP64;  // the staged pooling kernel is FP64
+  const qmc_wf_desc* d = &dd;
   if (nw < 0 || ld < d->nmo_used || (nw > 0 && (!mo || !dets || !scratch))) return QMC_ERR_ARG;
   if (bop && !op) return QMC_ERR_ARG;
   if (nw == 0) return QMC_OK;
   if (scratch_bytes < qmc_scratch_bytes(d, nw, 1)) return QMC_ERR_SCRATCH;
   const int64_t ss = pad_walkers(nw);
   const dim3 grid((unsigned)((nw + kTPB - 1) / kTPB));
+  unsigned char* scr = (unsigned char*)scratch;
   if (bop)
-    slater_kernel<true><<<grid, kTPB, 0, (cudaStream_t)stream>>>(*d, mo, bop, ld, nw, dets, op,
-                                                                 (double*)scratch, ss);
+    slater_kernel<true><<<grid, kTPB, 0, (cudaStream_t)stream>>>(dd, mo, bop, ld, nw, dets, op, scr,
+                                                                 ss);
   else
-    slater_kernel<false><<<grid, kTPB, 0, (cudaStream_t)stream>>>(*d, mo, nullptr, ld, nw, dets,
-                                                                  nullptr, (double*)scratch, ss);
+    slater_kernel<false><<<grid, kTPB, 0, (cudaStream_t)stream>>>(dd, mo, nullptr, ld, nw, dets,
+                                                                  nullptr, scr, ss);
   return launch_status();
 }
 

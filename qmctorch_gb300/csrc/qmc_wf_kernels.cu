@@ -1,46 +1,91 @@
-// Fused psi and local-energy kernels (FP64 plain method).
+// Fused psi and local-energy kernels (plain FP64 and mixed methods).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include <mutex>
 
+#include "qmc_ep.cuh"
 #include "qmc_host.cuh"
 
 namespace qmc {
 
 // ---------------------------------------------------------------------------
-// fused psi / local energy
+// fused psi / local energy (electron-parallel blocks, qmc_ep.cuh)
 // ---------------------------------------------------------------------------
-template <int JC>
-__global__ void __launch_bounds__(kTPB) psi_kernel(const qmc_wf_desc d, const double* __restrict__ pos,
-                                                   int64_t nw, double* __restrict__ psi,
-                                                   double* __restrict__ scr, int64_t ss) {
+template <typename R, int JC>
+__global__ void __launch_bounds__(EPBound<R>::kThreads) ep_psi_kernel(const qmc_wf_desc d, const double* __restrict__ pos,
+                                                      int64_t nw, double* __restrict__ psi,
+                                                      unsigned char* __restrict__ scr, int64_t ss,
+                                                      const EPShape S) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables t = load_tables(d, d.nmo_used, smem);
-  const Layout L = scratch_layout(d, 0);
-  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= nw) return;
-  PosView P{pos + w * 3 * d.nelec, 1};
-  psi[w] = walker_psi<JC>(d, t, L, P, scr + w, ss);
+  const Tables<R> t = load_tables<R>(d, d.nmo_used, smem + S.o_tab);
+  const int64_t w0 = (int64_t)blockIdx.x * S.nwb;
+  double* P = reinterpret_cast<double*>(smem + S.o_pos);
+  ep_stage_positions(pos, w0, nw, S.nwb, 3 * d.nelec, P);
+  ep_eval<R, JC, false>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
+  const int tid = threadIdx.x;
+  if (tid < S.nwb && w0 + tid < nw)
+    psi[w0 + tid] = reinterpret_cast<const double*>(smem + S.o_psi)[tid];
 }
 
-template <int JC>
-__global__ void __launch_bounds__(kTPB) eloc_kernel(const qmc_wf_desc d, const double* __restrict__ pos,
-                                                    int64_t nw, double* __restrict__ eloc,
-                                                    double* __restrict__ kin,
-                                                    double* __restrict__ psi,
-                                                    double* __restrict__ scr, int64_t ss) {
+template <typename R, int JC>
+__global__ void __launch_bounds__(EPBound<R>::kThreads) ep_eloc_kernel(const qmc_wf_desc d, const double* __restrict__ pos,
+                                                       int64_t nw, double* __restrict__ eloc,
+                                                       double* __restrict__ kin,
+                                                       double* __restrict__ psi,
+                                                       unsigned char* __restrict__ scr, int64_t ss,
+                                                       const EPShape S) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables t = load_tables(d, d.nmo_used, smem);
-  const Layout L = scratch_layout(d, 1);
-  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= nw) return;
-  PosView P{pos + w * 3 * d.nelec, 1};
-  double k = 0.0, p = 0.0;
-  const double e = walker_eloc<JC>(d, t, L, P, scr + w, ss, &k, &p);
-  eloc[w] = e;
-  if (kin) kin[w] = k;
-  if (psi) psi[w] = p;
+  const Tables<R> t = load_tables<R>(d, d.nmo_used, smem + S.o_tab);
+  const int64_t w0 = (int64_t)blockIdx.x * S.nwb;
+  double* P = reinterpret_cast<double*>(smem + S.o_pos);
+  ep_stage_positions(pos, w0, nw, S.nwb, 3 * d.nelec, P);
+  ep_eval<R, JC, true>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
+  const int tid = threadIdx.x;
+  if (tid < S.nwb && w0 + tid < nw) {
+    const double k = reinterpret_cast<const double*>(smem + S.o_kin)[tid];
+    const double v = reinterpret_cast<const double*>(smem + S.o_v)[tid];
+    eloc[w0 + tid] = k + v + d.e_nuc;
+    if (kin) kin[w0 + tid] = k;
+    if (psi) psi[w0 + tid] = reinterpret_cast<const double*>(smem + S.o_psi)[tid];
+  }
+}
+
+template <typename R, typename K>
+static int launch_prepare(K kernel, const EPShape& S) {
+  if (S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
+  return prepare_smem(kernel, S.smem);
+}
+
+template <typename R, int JC>
+static int launch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, double* psi,
+                      unsigned char* scr, cudaStream_t s) {
+  const EPShape S = ep_choose<R>(*d, 0);
+  int st = launch_prepare<R>(ep_psi_kernel<R, JC>, S);
+  if (st) return st;
+  const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
+  ep_psi_kernel<R, JC><<<grid, S.nthreads, S.smem, s>>>(*d, pos, nw, psi, scr, pad_walkers(nw), S);
+  return launch_status();
+}
+
+template <typename R>
+static int dispatch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, double* psi,
+                        unsigned char* scr, cudaStream_t s) {
+  if (d->nmo_used <= 8) return launch_psi<R, 8>(d, pos, nw, psi, scr, s);
+  if (d->nmo_used <= 16) return launch_psi<R, 16>(d, pos, nw, psi, scr, s);
+  return launch_psi<R, 24>(d, pos, nw, psi, scr, s);
+}
+
+template <typename R, int JC>
+static int launch_eloc(const qmc_wf_desc* d, const double* pos, int64_t nw, double* eloc,
+                       double* kin, double* psi, unsigned char* scr, cudaStream_t s) {
+  const EPShape S = ep_choose<R>(*d, 1);
+  int st = launch_prepare<R>(ep_eloc_kernel<R, JC>, S);
+  if (st) return st;
+  const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
+  ep_eloc_kernel<R, JC><<<grid, S.nthreads, S.smem, s>>>(*d, pos, nw, eloc, kin, psi, scr,
+                                                         pad_walkers(nw), S);
+  return launch_status();
 }
 
 }  // namespace qmc
@@ -56,22 +101,10 @@ int qmc_wf_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, double* psi,
   if (nw < 0 || (nw > 0 && (!pos || !psi || !scratch))) return QMC_ERR_ARG;
   if (nw == 0) return QMC_OK;
   if (scratch_bytes < qmc_scratch_bytes(d, nw, 0)) return QMC_ERR_SCRATCH;
-  const int64_t smem = tables_smem_bytes(*d, d->nmo_used);
-  const int64_t ss = pad_walkers(nw);
-  const dim3 grid((unsigned)((nw + kTPB - 1) / kTPB));
+  unsigned char* scr = (unsigned char*)scratch;
   cudaStream_t s = (cudaStream_t)stream;
-  double* scr = (double*)scratch;
-  if (d->nmo_used <= 8) {
-    if ((st = prepare_smem(psi_kernel<8>, smem))) return st;
-    psi_kernel<8><<<grid, kTPB, smem, s>>>(*d, pos, nw, psi, scr, ss);
-  } else if (d->nmo_used <= 16) {
-    if ((st = prepare_smem(psi_kernel<16>, smem))) return st;
-    psi_kernel<16><<<grid, kTPB, smem, s>>>(*d, pos, nw, psi, scr, ss);
-  } else {
-    if ((st = prepare_smem(psi_kernel<24>, smem))) return st;
-    psi_kernel<24><<<grid, kTPB, smem, s>>>(*d, pos, nw, psi, scr, ss);
-  }
-  return launch_status();
+  if (d->precision == QMC_PREC_MIXED) return dispatch_psi<float>(d, pos, nw, psi, scr, s);
+  return dispatch_psi<double>(d, pos, nw, psi, scr, s);
 }
 
 int qmc_wf_local_energy(const qmc_wf_desc* d, const double* pos, int64_t nw, double* eloc,
@@ -82,13 +115,11 @@ int qmc_wf_local_energy(const qmc_wf_desc* d, const double* pos, int64_t nw, dou
   if (nw < 0 || (nw > 0 && (!pos || !eloc || !scratch))) return QMC_ERR_ARG;
   if (nw == 0) return QMC_OK;
   if (scratch_bytes < qmc_scratch_bytes(d, nw, 1)) return QMC_ERR_SCRATCH;
-  const int64_t smem = tables_smem_bytes(*d, d->nmo_used);
-  if ((st = prepare_smem(eloc_kernel<8>, smem))) return st;
-  const int64_t ss = pad_walkers(nw);
-  const dim3 grid((unsigned)((nw + kTPB - 1) / kTPB));
-  eloc_kernel<8><<<grid, kTPB, smem, (cudaStream_t)stream>>>(*d, pos, nw, eloc, kinetic, psi,
-                                                              (double*)scratch, ss);
-  return launch_status();
+  unsigned char* scr = (unsigned char*)scratch;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (d->precision == QMC_PREC_MIXED)
+    return launch_eloc<float, 8>(d, pos, nw, eloc, kinetic, psi, scr, s);
+  return launch_eloc<double, 8>(d, pos, nw, eloc, kinetic, psi, scr, s);
 }
 
 }  // extern "C"

@@ -65,7 +65,7 @@ class Call:
 
 
 def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None, nup=None,
-               ndown=None, nmo_used=None, e_nuc=0.0):
+               ndown=None, nmo_used=None, e_nuc=0.0, precision=0):
     """Fill a ``qmc_wf_desc`` from the modules of a wave function. Any module
     may be absent (a standalone AO or Jastrow call); its fields then point to
     placeholders the called kernel does not read."""
@@ -131,4 +131,5 @@ def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None
     else:
         d.ci_weight = ptr(dd)
     d.e_nuc = float(e_nuc)
+    d.precision = int(precision)
     return Call(d, keep)

@@ -66,11 +66,26 @@ class WaveFunction(nn.Module):
         self.load_state_dict(data)
 
 
+PRECISIONS = {"fp64": 0, "mixed": 1}
+
+
 class SlaterJastrow(WaveFunction):
+    """``precision`` (keyword added to the reference signature) selects the
+    arithmetic of the fused psi / local-energy / Metropolis kernels: "fp64"
+    (the plain method) or "mixed" (FP32 AO, AO->MO, Jastrow and Slater LU;
+    FP64 determinant products, sums and one refinement step of the solves
+    feeding the kinetic energy). Default: "fp64" when torch's default dtype is
+    float64, else "mixed" (the reference's single-precision switch)."""
+
     def __init__(self, mol, jastrow="default", backflow=None, configs="ground_state",
                  kinetic="jacobi", cuda=False, include_all_mo=True, mix_mo=False,
-                 orthogonalize_mo=False):
+                 orthogonalize_mo=False, precision=None):
         super().__init__(mol.nelec, 3, kinetic, cuda)
+        if precision is None:
+            precision = "fp64" if torch.get_default_dtype() == torch.float64 else "mixed"
+        if precision not in PRECISIONS:
+            raise ValueError("precision must be 'fp64' or 'mixed'")
+        self.precision = precision
         if backflow is not None:
             raise NotImplementedError("backflow orbitals are not on the GB300 path")
         if not include_all_mo and isinstance(configs, str) and configs.startswith("cas("):
@@ -140,7 +155,8 @@ class SlaterJastrow(WaveFunction):
         return rt.build_desc(device, self.ao, mo=self.mo, pool=self.pool,
                              jastrow=self.jastrow if self.use_jastrow else None, fc=self.fc,
                              nup=self.mol.nup, ndown=self.mol.ndown,
-                             nmo_used=self.highest_occ_mo, e_nuc=self.nuclear_repulsion())
+                             nmo_used=self.highest_occ_mo, e_nuc=self.nuclear_repulsion(),
+                             precision=PRECISIONS[self.precision])
 
     # -- fused evaluations ----------------------------------------------------
     def _psi(self, pos):

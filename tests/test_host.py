@@ -92,7 +92,7 @@ def test_scratch_sizes_and_argument_checks(name):
     b0 = lib.qmc_scratch_bytes(ctypes.byref(desc), 1000, 0)
     b1 = lib.qmc_scratch_bytes(ctypes.byref(desc), 1000, 1)
     bm = lib.qmc_metropolis_scratch_bytes(ctypes.byref(desc), 1000)
-    assert 0 < b0 < b1 and b0 < bm
+    assert 0 < b0 < b1 and b0 <= bm
     assert b0 % (8 * 1024) == 0  # 1000 walkers padded to 1024 slots
     # argument errors are reported, never launched (no GPU needed)
     assert lib.qmc_wf_psi(ctypes.byref(desc), None, 10, None, None, 0, None) == 1
