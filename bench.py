@@ -41,11 +41,11 @@ L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 def parse():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=10)
+    p.add_argument("--steps", type=int, default=8)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--nwalkers", type=int, default=16384)
-    p.add_argument("--mc-steps", type=int, default=10)
+    p.add_argument("--mc-steps", type=int, default=100)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     return p.parse_args()
 
@@ -123,7 +123,7 @@ class ClockSampler:
             self.f = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
-                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                 "--format=csv,noheader,nounits", "-lms", "100"], stdout=self.f,
                 stderr=subprocess.DEVNULL)
         except (OSError, FileNotFoundError):
             self.proc = None
@@ -144,7 +144,7 @@ class ClockSampler:
         sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
         mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in rows for i in range(4) if "Active" in r[5 + i]})
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i] == "Active"})
         return {"sm_mhz": float(np.median(sm)) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None, "reasons": reasons, "samples": len(rows)}
 
@@ -195,7 +195,48 @@ def count_fp64_flops_per_psi(wf):
     return flops, exps
 
 
+def _timed(torch, fn, steps, flush):
+    """CUDA-event time (s) of `steps` calls of fn(i) on the current stream,
+    L2 flushed (outside the events) before each call."""
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(steps)]
+    for i in range(steps):
+        flush.fill_(float(i))
+        ev[i][0].record()
+        fn(i)
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    return sum(a.elapsed_time(b) for a, b in ev) / 1e3
+
+
+def precision_study(torch, wf64, wfm, x_eq, sampler, nfixed=100_000):
+    """Per-walker psi / E_L error of the mixed method against the FP64 method
+    on `nfixed` fixed positions (snapshots of an equilibrated FP64 chain)."""
+    snaps, n = [], 0
+    x = x_eq.clone()
+    while n < nfixed:
+        sampler.advance(wf64.pdf, x, nstep=10)
+        snaps.append(x.clone())
+        n += x.shape[0]
+    X = torch.cat(snaps)[:nfixed]
+    e64 = wf64.local_energy(X).reshape(-1).double()
+    em = wfm.local_energy(X).reshape(-1).double()
+    p64 = wf64(X).reshape(-1).double()
+    pm = wfm(X).reshape(-1).double()
+    de = (em - e64).abs()
+    dp = ((pm - p64) / p64).abs()
+    return {"n_positions": int(nfixed),
+            "mean_eloc_fp64": float(e64.mean()), "mean_eloc_mixed": float(em.mean()),
+            "mean_eloc_diff_ha": float(em.mean() - e64.mean()),
+            "eloc_abs_err_median_ha": float(de.median()), "eloc_abs_err_p99_ha": float(torch.quantile(de.float(), 0.99)),
+            "eloc_abs_err_max_ha": float(de.max()),
+            "psi_rel_err_median": float(dp.median()), "psi_rel_err_max": float(dp.max()),
+            "stat_error_of_mean_ha": float(e64.std() / nfixed ** 0.5)}
+
+
 def run_gb300(args):
+    import ctypes
+
     import torch
     import torch.distributed as dist
 
@@ -203,7 +244,7 @@ def run_gb300(args):
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     cpu = None
-    if rank == 0 and world >= 1:
+    if rank == 0:
         cpu = cpu_baseline(args.cpu_seconds)  # spawn pool before the first CUDA call
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
@@ -218,18 +259,15 @@ def run_gb300(args):
     torch.set_default_dtype(torch.float64)
     lib = _lib.lib()
     mol = Molecule(H2O, unit="angs", basis="cc-pvdz")
-    wf = SlaterJastrow(mol, configs=CONFIGS, cuda=True)
-    fc = np.random.default_rng(7).uniform(size=wf.nci)
-    wf.fc.weight.data = torch.as_tensor(fc, device=device).reshape(1, -1)
+    wf64 = SlaterJastrow(mol, configs=CONFIGS, cuda=True, precision="fp64")
+    fc = np.random.default_rng(7).uniform(size=wf64.nci)
+    wf64.fc.weight.data = torch.as_tensor(fc, device=device).reshape(1, -1)
+    wfm = SlaterJastrow(mol, configs=CONFIGS, cuda=True, precision="mixed")
+    wfm.load_state_dict(wf64.state_dict())
     nw = args.nwalkers
-    x = torch.as_tensor(seeded_positions(mol, nw, seed=rank), device=device)
-    sampler = Metropolis(nwalkers=nw, nstep=args.mc_steps, step_size=STEP_SIZE, nelec=mol.nelec,
-                         init=mol.domain("atomic"), cuda=True, seed=1234 + rank)
+    x0 = torch.as_tensor(seeded_positions(mol, nw, seed=rank), device=device)
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
-    call = wf._desc(device)
-    scr = torch.empty(lib.qmc_metropolis_scratch_bytes(call.ref, nw), dtype=torch.uint8,
-                      device=device)
-    acc = torch.zeros(nw, dtype=torch.int32, device=device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     peaks = probe_peaks(torch, lib, device)
 
     def barrier():
@@ -237,115 +275,120 @@ def run_gb300(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # warm-up (also equilibrates the walkers)
-    for _ in range(args.warmup):
-        sampler.advance(wf.pdf, x, accepted=acc, scratch=scr)
-    wf.local_energy(x)
+    def sampler_for(seed):
+        return Metropolis(nwalkers=nw, nstep=args.mc_steps, step_size=STEP_SIZE,
+                          nelec=mol.nelec, init=mol.domain("atomic"), cuda=True, seed=seed)
+
+    # equilibrate once with the FP64 chain; both methods start from these walkers
+    eq = sampler_for(4321 + rank)
+    x_eq = x0.clone()
+    eq.advance(wf64.pdf, x_eq, nstep=500)
     barrier()
 
+    results = {}
     clocks = ClockSampler(local)
     clocks.start()
-    # --- device-resident Metropolis: K timed launches, L2 flushed between ---
-    acc.zero_()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-          for _ in range(args.steps)]
-    barrier()
-    t0 = time.perf_counter()
-    for i in range(args.steps):
-        flush.fill_(float(i))
-        ev[i][0].record()
-        sampler.advance(wf.pdf, x, accepted=acc, scratch=scr)
-        ev[i][1].record()
-    barrier()
-    wall_met = time.perf_counter() - t0
-    met_ms = [a.elapsed_time(b) for a, b in ev]
-    # --- local energies of the same walkers ---
-    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
-           for _ in range(args.steps)]
-    el_call = wf._desc(device)
-    el_scr = torch.empty(lib.qmc_scratch_bytes(el_call.ref, nw, 1), dtype=torch.uint8,
-                         device=device)
-    eloc = torch.empty(nw, dtype=torch.float64, device=device)
-    import ctypes
-    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    barrier()
-    for i in range(args.steps):
-        flush.fill_(float(i))
-        ev2[i][0].record()
-        _lib.check(lib.qmc_wf_local_energy(el_call.ref, ctypes.c_void_p(x.data_ptr()), nw,
-                                           ctypes.c_void_p(eloc.data_ptr()), None, None,
-                                           ctypes.c_void_p(el_scr.data_ptr()), el_scr.numel(),
-                                           stream), "qmc_wf_local_energy")
-        ev2[i][1].record()
-    barrier()
-    clk = clocks.stop()
-    el_ms = [a.elapsed_time(b) for a, b in ev2]
-    accept_rate = float(acc.sum()) / (nw * args.mc_steps * args.steps)
+    for name, wf in (("mixed", wfm), ("fp64", wf64)):
+        x = x_eq.clone()
+        s = sampler_for(1234 + rank)
+        call = wf._desc(device)
+        scr = torch.empty(lib.qmc_metropolis_scratch_bytes(call.ref, nw), dtype=torch.uint8,
+                          device=device)
+        acc = torch.zeros(nw, dtype=torch.int32, device=device)
+        for _ in range(args.warmup):
+            s.advance(wf.pdf, x, accepted=acc, scratch=scr)
+        acc.zero_()
+        barrier()
+        met_s = _timed(torch, lambda i: s.advance(wf.pdf, x, accepted=acc, scratch=scr),
+                       args.steps, flush)
+        el_scr = torch.empty(lib.qmc_scratch_bytes(call.ref, nw, 1), dtype=torch.uint8,
+                             device=device)
+        eloc = torch.empty(nw, dtype=torch.float64, device=device)
 
-    # --- end to end through the public API, host buffers ---
-    pos_host = x.detach().cpu().pin_memory()
-    sampler_e2e = Metropolis(nwalkers=nw, nstep=args.mc_steps, step_size=STEP_SIZE,
-                             nelec=mol.nelec, init=mol.domain("atomic"), cuda=False,
-                             seed=99 + rank)
-    out = sampler_e2e(wf.pdf, pos=pos_host, with_tqdm=False)  # warm
+        def el_call(i):
+            _lib.check(lib.qmc_wf_local_energy(call.ref, ctypes.c_void_p(x.data_ptr()), nw,
+                                               ctypes.c_void_p(eloc.data_ptr()), None, None,
+                                               ctypes.c_void_p(el_scr.data_ptr()),
+                                               el_scr.numel(), stream), "qmc_wf_local_energy")
+        el_call(0)
+        barrier()
+        el_s = _timed(torch, el_call, args.steps, flush)
+        results[name] = {"met_s": met_s, "el_s": el_s,
+                         "accept": float(acc.sum()) / (nw * args.mc_steps * args.steps)}
+    clk = clocks.stop()
+
+    prec = precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank)) if rank == 0 else None
+
+    # --- end to end through the public API (mixed method), host buffers ---
+    pos_host = x_eq.detach().cpu().pin_memory()
+    s_e2e = Metropolis(nwalkers=nw, nstep=args.mc_steps, step_size=STEP_SIZE, nelec=mol.nelec,
+                       init=mol.domain("atomic"), cuda=False, seed=99 + rank)
+    out = s_e2e(wfm.pdf, pos=pos_host, with_tqdm=False)
     barrier()
     t0 = time.perf_counter()
     for i in range(args.steps):
-        out = sampler_e2e(wf.pdf, pos=pos_host, with_tqdm=False)
+        out = s_e2e(wfm.pdf, pos=pos_host, with_tqdm=False)
     barrier()
     e2e_s = time.perf_counter() - t0
     h2d = pos_host.numel() * 8
     d2h = out.numel() * out.element_size() + pos_host.numel() * 8
 
-    # --- aggregate over ranks ---
-    met_s = sum(met_ms) / 1e3
-    el_s = sum(el_ms) / 1e3
-    loc = torch.tensor([met_s, el_s, e2e_s, wall_met], dtype=torch.float64, device=device)
+    vals = [results["mixed"]["met_s"], results["mixed"]["el_s"], results["fp64"]["met_s"],
+            results["fp64"]["el_s"], e2e_s]
+    loc = torch.tensor(vals, dtype=torch.float64, device=device)
     if world > 1:
         dist.all_reduce(loc, op=dist.ReduceOp.MAX)
-    met_s, el_s, e2e_s, wall_met = loc.tolist()
-    wsteps = nw * args.mc_steps * args.steps * world
-    value = wsteps / met_s
+    m_met, m_el, f_met, f_el, e2e_s = loc.tolist()
+    units = nw * args.mc_steps * args.steps
+    value = units * world / m_met
     if rank == 0:
-        flops, exps = count_fp64_flops_per_psi(wf)
-        per_launch_ms = met_s * 1e3 / args.steps
-        launch_wsteps = nw * args.mc_steps
-        achieved = flops * launch_wsteps / (per_launch_ms * 1e-3) / 1e9
+        flops, exps = count_fp64_flops_per_psi(wf64)
+        launch_units = nw * args.mc_steps
+        ach_m = flops * launch_units / (m_met / args.steps) / 1e9
+        ach_f = flops * launch_units / (f_met / args.steps) / 1e9
         line = {
-            "metric": "walker-steps/s (Metropolis all-electron; E_L/s alongside)",
+            "metric": "walker-steps/s (Metropolis all-electron, mixed-precision method; "
+                      "E_L/s and the plain FP64 method alongside)",
             "value": value,
             "unit": "walker-steps/s",
             "n_gpus": world,
             "steps": args.steps,
             "warmup": args.warmup,
-            "ms_per_step": met_s * 1e3 / args.steps,
+            "ms_per_step": m_met * 1e3 / args.steps,
             "higher_is_better": True,
             "scaling": "weak",
             "vs_baseline": None,
-            "dtype": "f64",
+            "dtype": "f32+f64 (mixed)",
             "data": "synthetic (seeded walker positions; built-in cc-pVDZ tables, extended-Hueckel MOs)",
             "config": {"workload": "h2o_ccpvdz_single_double44_16384w",
                        "molecule": "H2O cc-pVDZ (25 cart AOs, 10 e)", "configs": CONFIGS,
                        "nwalkers_per_gpu": nw, "mc_steps_per_step": args.mc_steps,
-                       "step_size": STEP_SIZE, "method": "plain FP64",
+                       "step_size": STEP_SIZE, "method": "mixed (FP32 + FP64 refinement)",
                        "l2": "flushed between timed steps (256 MB write)"},
-            "el_per_s": nw * args.steps * world / el_s,
-            "ms_per_eloc_batch": el_s * 1e3 / args.steps,
-            "acceptance": accept_rate,
-            "roofline": {"bound": "fp64", "kernel": "metropolis_kernel",
-                         "achieved": achieved, "peak": peaks["fp64_gflops"], "unit": "GFLOP/s",
-                         "frac": achieved / peaks["fp64_gflops"], "traffic": None,
+            "el_per_s": nw * args.steps * world / m_el,
+            "fp64": {"walker_steps_per_s": units * world / f_met,
+                     "el_per_s": nw * args.steps * world / f_el,
+                     "ms_per_step": f_met * 1e3 / args.steps},
+            "speedup_vs_fp64": {"walker_steps": f_met / m_met, "el": f_el / m_el},
+            "precision_vs_fp64": prec,
+            "acceptance": results["mixed"]["accept"],
+            "roofline": {"bound": "fp32", "kernel": "metropolis_kernel<float>",
+                         "achieved": ach_m, "peak": peaks["fp32_gflops"], "unit": "GFLOP/s",
+                         "frac": ach_m / peaks["fp32_gflops"], "traffic": None,
                          "flops_per_walker_step": flops, "exp_per_walker_step": exps,
-                         "peak_source": "in-run FP64 FMA probe (qmc_probe_fma); "
-                                        "MEASURED_PEAKS.json holds no FP64 figure"},
+                         "peak_source": "in-run FP32 FMA probe (qmc_probe_fma); "
+                                        "MEASURED_PEAKS.json holds HBM and BF16 figures only"},
+            "roofline_fp64": {"bound": "fp64", "kernel": "metropolis_kernel<double>",
+                              "achieved": ach_f, "peak": peaks["fp64_gflops"], "unit": "GFLOP/s",
+                              "frac": ach_f / peaks["fp64_gflops"]},
             "peaks_measured": peaks,
             "cpu_baseline": cpu,
-            "e2e": {"value": wsteps / e2e_s, "unit": "walker-steps/s",
+            "e2e": {"value": units * world / e2e_s, "unit": "walker-steps/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "api": "Metropolis.__call__(wf.pdf, pos=pinned host tensor) -> host samples"},
-            "gpu_launches": 2 * args.steps,
+                    "api": "Metropolis.__call__(wf.pdf, pos=pinned host tensor) -> host samples "
+                           "(mixed method)"},
+            "gpu_launches": 4 * args.steps,
             "clocks": clk,
-            "wall_s_metropolis": wall_met,
         }
         print(json.dumps(line))
     if world > 1:

@@ -13,6 +13,10 @@
 //   3. combine phase (threads < nwb): CI sum, Jastrow factor, energies.
 // Compared with one thread per walker this gives nelec times more threads
 // (about 34 warps per SM for 16384 H2O walkers) to hide FP32 and L1 latency.
+//
+// Positions live in shared memory as split coordinates XP<R> (see
+// qmc_device.cuh): FP64 values for the plain method, FP32 pairs h + l for the
+// mixed method, so that every difference in the inner loops is FP32 work.
 #pragma once
 
 #include "qmc_device.cuh"
@@ -25,26 +29,30 @@ namespace qmc {
 struct EPShape {
   int nwb;       // walkers per block
   int nthreads;  // threads per block
+  int ncol;      // W columns stored per AO (nmo_used rounded up to the MO chunk)
   int64_t smem;  // dynamic shared memory bytes
   int64_t o_tab, o_pos, o_pnew, o_mo, o_bk, o_jrow, o_vrow, o_dref, o_psi, o_f, o_kin, o_v,
       o_iel, o_acc;
 };
 
 template <typename R>
-__host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb) {
+__host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb, int jc) {
   EPShape s;
   s.nwb = nwb;
   int nt = nwb * d.nelec;
   if (nt < 2 * nwb) nt = 2 * nwb;
   s.nthreads = ((nt + 31) / 32) * 32;
+  s.ncol = round_up(d.nmo_used, jc);
   const int64_t nc = 3 * (int64_t)d.nelec, nmu = d.nmo_used;
+  const int64_t xps = 2 * (int64_t)sizeof(R);  // bytes of one split coordinate
   int64_t o = 0;
   s.o_tab = o;
-  o += tables_smem_bytes<R>(d, d.nmo_used);
+  o += tables_smem_bytes<R>(d, s.ncol);
+  o = (o + 15) & ~int64_t(15);
   s.o_pos = o;
-  o += align8(nwb * nc * 8);
+  o += align8(nwb * nc * xps);
   s.o_pnew = o;
-  if (kind == 2) o += align8(nwb * nc * 8);
+  if (kind == 2) o += align8(nwb * nc * xps);
   s.o_mo = o;
   o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
   s.o_bk = o;
@@ -80,15 +88,17 @@ struct EPBound {
 
 // Largest walkers-per-block that fits the shared memory and the thread bound.
 template <typename R>
-__host__ inline EPShape ep_choose(const qmc_wf_desc& d, int kind) {
+__host__ inline EPShape ep_choose(const qmc_wf_desc& d, int kind, int jc) {
   for (int nwb = 32; nwb > 1; nwb /= 2) {
-    const EPShape s = ep_shape<R>(d, kind, nwb);
+    const EPShape s = ep_shape<R>(d, kind, nwb, jc);
     if (s.nthreads <= EPBound<R>::kThreads && s.smem <= 200 * 1024) return s;
   }
-  return ep_shape<R>(d, kind, 1);
+  return ep_shape<R>(d, kind, 1, jc);
 }
 
-// Per-walker scratch: the determinant-phase work arrays of both spins.
+// Per-walker scratch: the determinant-phase work arrays of both spins. The
+// relative determinant values are FP64 for the local energy and of the
+// compute type for psi.
 struct EPLayout {
   Region lu[2], x[2], y[2], x64[2], y64[2], rc[2], dv, ov;
   int64_t bytes_per_slot;
@@ -114,6 +124,7 @@ __host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
     r.off = o;
     r.esize = esize;
     o += count * esize;
+    o = align8(o);
   };
   const bool el = kind == 1;
   for (int s = 0; s < 2; ++s) {
@@ -124,37 +135,21 @@ __host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
     add(L.y64[s], (el && mixed) ? (int64_t)nmax * omax : 0, 8);
     add(L.rc[s], (el && mixed) ? nmax : 0, rsz);
   }
-  add(L.dv, d.ndet[0] + d.ndet[1], 8);
+  add(L.dv, d.ndet[0] + d.ndet[1], el ? 8 : rsz);
   add(L.ov, el ? d.ndet[0] + d.ndet[1] : 0, 8);
-  L.bytes_per_slot = align8(o);
+  L.bytes_per_slot = o;
   return L;
 }
 
 // ---------------------------------------------------------------------------
-// AO groups, specialised by component count
+// AO groups
 // ---------------------------------------------------------------------------
-// x^k and its first / second derivatives for the cartesian powers of s, p, d
-// shells by selects (no loop); larger powers fall back to ipow.
-template <typename R>
-__device__ __forceinline__ R pk0(R x, int k) {
-  return k == 0 ? (R)1 : (k == 1 ? x : (k == 2 ? x * x : ipow(x, k)));
-}
-template <typename R>
-__device__ __forceinline__ R pk1(R x, int k) {
-  return k == 0 ? (R)0 : (k == 1 ? (R)1 : (k == 2 ? (R)2 * x : (R)k * ipow(x, k - 1)));
-}
-template <typename R>
-__device__ __forceinline__ R pk2(R x, int k) {
-  return k < 2 ? (R)0 : (k == 2 ? (R)2 : (R)(k * (k - 1)) * ipow(x, k - 2));
-}
-
-template <typename R, bool DERIV, int NC, typename F>
-__device__ __forceinline__ void group_eval(const Tables<R>& t, int g, R dx, R dy, R dz, R r2,
-                                           F& f) {
+// Radial sums G_n = sum_p w_cp alpha_p^n exp(-alpha_p r^2) of NC components.
+template <typename R, bool DERIV, int NC>
+__device__ __forceinline__ void group_radial(const Tables<R>& t, int g, R r2, R (&G0)[NC],
+                                             R (&G1)[NC], R (&G2)[NC]) {
   const int p0 = t.group_prim[g], np = t.group_prim[g + 1] - p0;
-  const int a0 = t.group_ao[g];
-  const int wb = t.ao_wofs[a0];  // weights of component c at wb + c * np
-  R G0[NC], G1[NC], G2[NC];
+  const int wb = t.ao_wofs[t.group_ao[g]];  // weights of component c at wb + c * np
 #pragma unroll
   for (int c = 0; c < NC; ++c) G0[c] = G1[c] = G2[c] = (R)0;
   for (int p = 0; p < np; ++p) {
@@ -171,67 +166,183 @@ __device__ __forceinline__ void group_eval(const Tables<R>& t, int g, R dx, R dy
       }
     }
   }
+}
+
+// AO from its polynomial P (gradient dP, laplacian lapP, degree l) and the
+// radial sums: val = P G0, grad = dP G0 - 2 r P G1,
+// lap = lapP G0 + P (4 r^2 G2 - (6 + 4 l) G1) (Euler: r . grad P = l P).
+template <typename R, bool DERIV>
+__device__ __forceinline__ AOVal<R> ao_from(R P, R px, R py, R pz, R lapP, int l, R dx, R dy, R dz,
+                                            R r2, R g0, R g1, R g2, R vs) {
+  AOVal<R> o;
+  o.v = vs * (P * g0);
+  if (DERIV) {
+    const R pg1 = (R)(-2) * P * g1;
+    o.gx = fma(px, g0, dx * pg1);
+    o.gy = fma(py, g0, dy * pg1);
+    o.gz = fma(pz, g0, dz * pg1);
+    o.lap = vs * fma(lapP, g0, P * ((R)4 * r2 * g2 - (R)(6 + 4 * l) * g1));
+  }
+  return o;
+}
+
+// x^k, d/dx x^k, d2/dx2 x^k by selects (loops only for k > 2).
+template <typename R>
+__device__ __forceinline__ R pk0(R x, int k) {
+  return k == 0 ? (R)1 : (k == 1 ? x : (k == 2 ? x * x : ipow(x, k)));
+}
+template <typename R>
+__device__ __forceinline__ R pk1(R x, int k) {
+  return k == 0 ? (R)0 : (k == 1 ? (R)1 : (k == 2 ? (R)2 * x : (R)k * ipow(x, k - 1)));
+}
+template <typename R>
+__device__ __forceinline__ R pk2(R x, int k) {
+  return k < 2 ? (R)0 : (k == 2 ? (R)2 : (R)(k * (k - 1)) * ipow(x, k - 2));
+}
+
+template <typename R, bool DERIV, int NC, typename F>
+__device__ __forceinline__ void group_generic(const Tables<R>& t, int g, R dx, R dy, R dz, R r2,
+                                              F& f) {
+  R G0[NC], G1[NC], G2[NC];
+  group_radial<R, DERIV, NC>(t, g, r2, G0, G1, G2);
+  const int a0 = t.group_ao[g];
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
     const int a = a0 + c;
     const int kx = t.ao_k[3 * a], ky = t.ao_k[3 * a + 1], kz = t.ao_k[3 * a + 2];
     const R px = pk0(dx, kx), py = pk0(dy, ky), pz = pk0(dz, kz);
-    const R P = px * py * pz;
-    const R vs = t.vscale ? t.vscale[a] : (R)1;
-    AOVal<R> o;
-    o.v = vs * (P * G0[c]);
+    R qx = 0, qy = 0, qz = 0, lapP = 0;
     if (DERIV) {
-      const R qx = pk1(dx, kx), qy = pk1(dy, ky), qz = pk1(dz, kz);
-      const R lapP = pk2(dx, kx) * py * pz + px * pk2(dy, ky) * pz + px * py * pk2(dz, kz);
-      const R pg1 = (R)(-2) * P * G1[c];
-      o.gx = fma(qx * py * pz, G0[c], dx * pg1);
-      o.gy = fma(px * qy * pz, G0[c], dy * pg1);
-      o.gz = fma(px * py * qz, G0[c], dz * pg1);
-      const int l = kx + ky + kz;
-      o.lap = vs * fma(lapP, G0[c], P * ((R)4 * r2 * G2[c] - (R)(6 + 4 * l) * G1[c]));
+      qx = pk1(dx, kx) * py * pz;
+      qy = px * pk1(dy, ky) * pz;
+      qz = px * py * pk1(dz, kz);
+      lapP = pk2(dx, kx) * py * pz + px * pk2(dy, ky) * pz + px * py * pk2(dz, kz);
     }
-    f(a, o);
+    const R vs = t.vscale ? t.vscale[a] : (R)1;
+    f(a, ao_from<R, DERIV>(px * py * pz, qx, qy, qz, lapP, kx + ky + kz, dx, dy, dz, r2, G0[c],
+                           G1[c], G2[c], vs));
   }
 }
 
-// All AOs of one electron; the electron-atom difference is formed once per
-// atom (groups are stored atom by atom).
+template <typename R, bool DERIV, int NC, typename F>
+__device__ __forceinline__ void group_s(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
+  R G0[NC], G1[NC], G2[NC];
+  group_radial<R, DERIV, NC>(t, g, r2, G0, G1, G2);
+  const int a0 = t.group_ao[g];
+#pragma unroll
+  for (int c = 0; c < NC; ++c) {
+    const R vs = t.vscale ? t.vscale[a0 + c] : (R)1;
+    f(a0 + c, ao_from<R, DERIV>((R)1, (R)0, (R)0, (R)0, (R)0, 0, dx, dy, dz, r2, G0[c], G1[c],
+                                G2[c], vs));
+  }
+}
+
 template <typename R, bool DERIV, typename F>
-__device__ __forceinline__ void for_each_ao_ep(const Tables<R>& t, double ex, double ey,
-                                               double ez, F&& f) {
+__device__ __forceinline__ void group_p(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
+  R G0[3], G1[3], G2[3];
+  group_radial<R, DERIV, 3>(t, g, r2, G0, G1, G2);
+  const int a0 = t.group_ao[g];
+  const R o = (R)0, i = (R)1;
+  auto vs = [&](int c) { return t.vscale ? t.vscale[a0 + c] : (R)1; };
+  f(a0, ao_from<R, DERIV>(dx, i, o, o, o, 1, dx, dy, dz, r2, G0[0], G1[0], G2[0], vs(0)));
+  f(a0 + 1, ao_from<R, DERIV>(dy, o, i, o, o, 1, dx, dy, dz, r2, G0[1], G1[1], G2[1], vs(1)));
+  f(a0 + 2, ao_from<R, DERIV>(dz, o, o, i, o, 1, dx, dy, dz, r2, G0[2], G1[2], G2[2], vs(2)));
+}
+
+// cartesian d shell, components xx, xy, xz, yy, yz, zz (pyscf.py:120-122)
+template <typename R, bool DERIV, typename F>
+__device__ __forceinline__ void group_d(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
+  R G0[6], G1[6], G2[6];
+  group_radial<R, DERIV, 6>(t, g, r2, G0, G1, G2);
+  const int a0 = t.group_ao[g];
+  const R o = (R)0, two = (R)2;
+  auto vs = [&](int c) { return t.vscale ? t.vscale[a0 + c] : (R)1; };
+  f(a0, ao_from<R, DERIV>(dx * dx, two * dx, o, o, two, 2, dx, dy, dz, r2, G0[0], G1[0], G2[0],
+                          vs(0)));
+  f(a0 + 1, ao_from<R, DERIV>(dx * dy, dy, dx, o, o, 2, dx, dy, dz, r2, G0[1], G1[1], G2[1],
+                              vs(1)));
+  f(a0 + 2, ao_from<R, DERIV>(dx * dz, dz, o, dx, o, 2, dx, dy, dz, r2, G0[2], G1[2], G2[2],
+                              vs(2)));
+  f(a0 + 3, ao_from<R, DERIV>(dy * dy, o, two * dy, o, two, 2, dx, dy, dz, r2, G0[3], G1[3], G2[3],
+                              vs(3)));
+  f(a0 + 4, ao_from<R, DERIV>(dy * dz, o, dz, dy, o, 2, dx, dy, dz, r2, G0[4], G1[4], G2[4],
+                              vs(4)));
+  f(a0 + 5, ao_from<R, DERIV>(dz * dz, o, o, two * dz, two, 2, dx, dy, dz, r2, G0[5], G1[5], G2[5],
+                              vs(5)));
+}
+
+// All AOs of one electron (split coordinates ex, ey, ez); the electron-atom
+// difference is formed once per atom (groups are stored atom by atom).
+template <typename R, bool DERIV, typename F>
+__device__ __forceinline__ void for_each_ao_ep(const Tables<R>& t, XP<R> ex, XP<R> ey, XP<R> ez,
+                                               F& f) {
   int last = -1;
   R dx = 0, dy = 0, dz = 0, r2 = 0;
   for (int g = 0; g < t.ngroup; ++g) {
     const int A = t.group_atom[g];
     if (A != last) {
-      dx = (R)(ex - t.atom_xyz[3 * A]);
-      dy = (R)(ey - t.atom_xyz[3 * A + 1]);
-      dz = (R)(ez - t.atom_xyz[3 * A + 2]);
+      dx = dif(ex, t.atom_p[3 * A]);
+      dy = dif(ey, t.atom_p[3 * A + 1]);
+      dz = dif(ez, t.atom_p[3 * A + 2]);
       r2 = dx * dx + dy * dy + dz * dz;
       last = A;
     }
-    switch (t.group_ao[g + 1] - t.group_ao[g]) {
-      case 1: group_eval<R, DERIV, 1>(t, g, dx, dy, dz, r2, f); break;
-      case 2: group_eval<R, DERIV, 2>(t, g, dx, dy, dz, r2, f); break;
-      case 3: group_eval<R, DERIV, 3>(t, g, dx, dy, dz, r2, f); break;
-      case 4: group_eval<R, DERIV, 4>(t, g, dx, dy, dz, r2, f); break;
-      case 5: group_eval<R, DERIV, 5>(t, g, dx, dy, dz, r2, f); break;
-      default: group_eval<R, DERIV, 6>(t, g, dx, dy, dz, r2, f); break;
+    const int nc = t.group_ao[g + 1] - t.group_ao[g];
+    switch (t.group_kind[g]) {
+      case GK_S:
+        if (nc == 1) group_s<R, DERIV, 1>(t, g, dx, dy, dz, r2, f);
+        else if (nc == 2) group_s<R, DERIV, 2>(t, g, dx, dy, dz, r2, f);
+        else group_generic<R, DERIV, QMC_MAX_COMP>(t, g, dx, dy, dz, r2, f);
+        break;
+      case GK_P: group_p<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
+      case GK_D: group_d<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
+      default:
+        switch (nc) {
+          case 1: group_generic<R, DERIV, 1>(t, g, dx, dy, dz, r2, f); break;
+          case 2: group_generic<R, DERIV, 2>(t, g, dx, dy, dz, r2, f); break;
+          case 3: group_generic<R, DERIV, 3>(t, g, dx, dy, dz, r2, f); break;
+          case 4: group_generic<R, DERIV, 4>(t, g, dx, dy, dz, r2, f); break;
+          case 5: group_generic<R, DERIV, 5>(t, g, dx, dy, dz, r2, f); break;
+          default: group_generic<R, DERIV, 6>(t, g, dx, dy, dz, r2, f); break;
+        }
     }
+  }
+}
+
+// JC consecutive W values with vector loads (rows are 16-byte aligned and
+// padded to a multiple of JC).
+template <int JC>
+__device__ __forceinline__ void load_w(const float* p, float (&w)[JC]) {
+#pragma unroll
+  for (int q = 0; q < JC / 4; ++q) {
+    const float4 v = reinterpret_cast<const float4*>(p)[q];
+    w[4 * q] = v.x;
+    w[4 * q + 1] = v.y;
+    w[4 * q + 2] = v.z;
+    w[4 * q + 3] = v.w;
+  }
+}
+template <int JC>
+__device__ __forceinline__ void load_w(const double* p, double (&w)[JC]) {
+#pragma unroll
+  for (int q = 0; q < JC / 2; ++q) {
+    const double2 v = reinterpret_cast<const double2*>(p)[q];
+    w[2 * q] = v.x;
+    w[2 * q + 1] = v.y;
   }
 }
 
 // ---------------------------------------------------------------------------
 // phase 1: one electron of one walker
 // ---------------------------------------------------------------------------
-// pw: the walker's positions (shared memory, FP64). mo / bk: element (e, j) of
-// this walker at [(e * nmu + j) * nwb]. jrow: log J partial of this electron;
-// vrow (E_L): its V_en plus half its V_ee row.
+// pw: the walker's split coordinates (shared memory). mo / bk: element (e, j)
+// of this walker at [(e * nmu + j) * nwb]. jrow: log J partial of this
+// electron; vrow (E_L): its V_en plus half its V_ee row.
 template <typename R, int JC, bool KIN>
-__device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, const double* pw,
+__device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, const XP<R>* pw,
                                    int e, R* mo, R* bk, int nwb, double* jrow, double* vrow) {
   const int ne = d.nelec, nmu = d.nmo_used;
-  const double ex = pw[3 * e], ey = pw[3 * e + 1], ez = pw[3 * e + 2];
+  const XP<R> ex = pw[3 * e], ey = pw[3 * e + 1], ez = pw[3 * e + 2];
   R gx = (R)0, gy = (R)0, gz = (R)0, jl = (R)0;
   {
     const R w = (R)__ldg(d.jastrow_w);
@@ -239,7 +350,7 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
     if (d.use_jastrow || KIN) {
       for (int j = KIN ? 0 : e + 1; j < ne; ++j) {
         if (j == e) continue;
-        const R dx = (R)(ex - pw[3 * j]), dy = (R)(ey - pw[3 * j + 1]), dz = (R)(ez - pw[3 * j + 2]);
+        const R dx = dif(ex, pw[3 * j]), dy = dif(ey, pw[3 * j + 1]), dz = dif(ez, pw[3 * j + 2]);
         const R r = rsqrt_(dx * dx + dy * dy + dz * dz);
         if (KIN) vs += (R)1 / r;
         if (d.use_jastrow) {
@@ -262,8 +373,8 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
       *jrow = 0.5 * (double)ks;               // every pair visited from both ends
       R ven = (R)0;
       for (int A = 0; A < t.natom; ++A) {
-        const R dx = (R)(ex - t.atom_xyz[3 * A]), dy = (R)(ey - t.atom_xyz[3 * A + 1]),
-                dz = (R)(ez - t.atom_xyz[3 * A + 2]);
+        const R dx = dif(ex, t.atom_p[3 * A]), dy = dif(ey, t.atom_p[3 * A + 1]),
+                dz = dif(ez, t.atom_p[3 * A + 2]);
         ven -= (R)t.atom_z[A] / rsqrt_(dx * dx + dy * dy + dz * dz);
       }
       *vrow = 0.5 * (double)vs + (double)ven;
@@ -279,18 +390,16 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
 #pragma unroll
     for (int jj = 0; jj < JC; ++jj) a0[jj] = ad[jj] = al[jj] = (R)0;
     auto acc = [&](int a, const AOVal<R>& o) {
-      const R* Wa = t.W + (int64_t)a * t.ncol + j0;
+      R wv[JC];
+      load_w<JC>(t.W + (int64_t)a * t.ncol + j0, wv);
       R gdot = (R)0;
       if (KIN) gdot = (R)2 * (gx * o.gx + gy * o.gy + gz * o.gz);
 #pragma unroll
       for (int jj = 0; jj < JC; ++jj) {
-        if (j0 + jj < nmu) {
-          const R wj = Wa[jj];
-          a0[jj] = fma(o.v, wj, a0[jj]);
-          if (KIN) {
-            ad[jj] = fma(gdot, wj, ad[jj]);
-            al[jj] = fma(o.lap, wj, al[jj]);
-          }
+        a0[jj] = fma(o.v, wv[jj], a0[jj]);
+        if (KIN) {
+          ad[jj] = fma(gdot, wv[jj], ad[jj]);
+          al[jj] = fma(o.lap, wv[jj], al[jj]);
         }
       }
     };
@@ -312,6 +421,7 @@ template <typename R, bool OP>
 __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned char* scr,
                               int64_t ss, int64_t w, int spin, const R* mo_s, const R* bk_s, int wl,
                               int nwb, double* dref) {
+  using T = typename std::conditional<OP, double, R>::type;
   const int row0 = spin ? d.nup : 0;
   const int64_t cs = nwb, rs = (int64_t)d.nmo_used * nwb;
   const CView<R> mo{mo_s + row0 * rs + wl, rs, cs};
@@ -324,9 +434,9 @@ __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned 
   wk.rc = MView<R>{rptr<R>(scr, L.rc[spin], ss, w), ss, ss};
   wk.X64 = MView<double>{rptr<double>(scr, L.x64[spin], ss, w), vm * ss, ss};
   wk.Y64 = MView<double>{rptr<double>(scr, L.y64[spin], ss, w), (int64_t)L.omax * ss, ss};
-  double* dv = rptr<double>(scr, L.dv, ss, w) + (spin ? d.ndet[0] * ss : 0);
+  T* dv = rptr<T>(scr, L.dv, ss, w) + (spin ? d.ndet[0] * ss : 0);
   double* ov = OP ? rptr<double>(scr, L.ov, ss, w) + (spin ? d.ndet[0] * ss : 0) : nullptr;
-  spin_channel<R, OP>(d, spin, mo, bk, wk, SpinOut{dv, ov, ss, &dref[spin * nwb + wl]});
+  spin_channel<R, OP, T>(d, spin, mo, bk, wk, SpinOut<T>{dv, ov, ss, &dref[spin * nwb + wl]});
 }
 
 struct EPPtrs {
@@ -335,12 +445,12 @@ struct EPPtrs {
 };
 
 // Evaluate psi (and, with KIN, the kinetic energy and potentials) for the
-// block's walkers at positions `pbuf` (shared memory, [nwb][3 nelec]).
+// block's walkers at split positions `pbuf` (shared memory, [nwb][3 nelec]).
 // Results in shared memory: psi[wl], and with KIN kin[wl], v[wl] (V_en + V_ee).
 // Every thread of the block must call this (it contains block barriers).
 template <typename R, int JC, bool KIN>
 __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const EPPtrs& p,
-                               const double* pbuf, unsigned char* scr, int64_t ss, int64_t w0,
+                               const XP<R>* pbuf, unsigned char* scr, int64_t ss, int64_t w0,
                                int64_t nw) {
   const EPShape& S = p.S;
   const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne;
@@ -367,13 +477,13 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   }
   __syncthreads();
   if (tid < nwb && w0 + tid < nw) {
+    using T = typename std::conditional<KIN, double, R>::type;
     const int wl = tid;
     const int64_t w = w0 + wl;
     double kin = 0.0;
-    const double* dv = rptr<double>(scr, L.dv, ss, w);
+    const T* dv = rptr<T>(scr, L.dv, ss, w);
     const double* ov = KIN ? rptr<double>(scr, L.ov, ss, w) : nullptr;
-    using A = typename std::conditional<KIN, double, R>::type;
-    const double psid = ci_combine<A, KIN>(d, dv, ov, ss, DREF[wl], DREF[nwb + wl], &kin);
+    const double psid = ci_combine<T, KIN, T>(d, dv, ov, ss, DREF[wl], DREF[nwb + wl], &kin);
     double logj = 0.0, v = 0.0;
     for (int e = 0; e < ne; ++e) {
       logj += JR[e * nwb + wl];
@@ -388,17 +498,41 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   __syncthreads();
 }
 
-// Stage the positions of walkers [w0, w0 + nwb) into shared memory; slots past
-// the last walker repeat walker nw - 1 (a valid configuration, never stored).
+// Stage the positions of walkers [w0, w0 + nwb) into shared memory as split
+// coordinates; slots past the last walker repeat walker nw - 1 (a valid
+// configuration, never stored).
+template <typename R>
 __device__ inline void ep_stage_positions(const double* pos, int64_t w0, int64_t nw, int nwb,
-                                          int nc, double* P) {
+                                          int nc, XP<R>* P) {
   for (int i = threadIdx.x; i < nwb * nc; i += blockDim.x) {
     const int wl = i / nc, c = i - wl * nc;
     int64_t w = w0 + wl;
     if (w >= nw) w = nw - 1;
-    P[i] = pos[w * nc + c];
+    P[i] = split_xp<R>(pos[w * nc + c]);
   }
   __syncthreads();
+}
+
+// x + dz for a split coordinate: FP64 addition (plain method) or an FP32
+// two-sum with renormalisation (mixed method; dl carries the part of a FP64
+// increment below FP32 precision, 0 for generated FP32 increments).
+template <typename R>
+__device__ __forceinline__ XP<R> xp_add(XP<R> x, R dz, R dl = (R)0) {
+  if constexpr (std::is_same<R, float>::value) {
+    const float s = x.h + dz;
+    const float bb = s - x.h;
+    const float err = (x.h - (s - bb)) + (dz - bb);
+    const float lo = x.l + err + dl;
+    const float h = s + lo;
+    return XP<R>{h, lo - (h - s)};
+  } else {
+    return XP<R>{x.h + dz, 0.0};
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ double xp_value(XP<R> x) {
+  return (double)x.h + (double)x.l;
 }
 
 }  // namespace qmc

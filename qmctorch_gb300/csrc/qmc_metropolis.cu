@@ -45,6 +45,15 @@ struct Rng {
     z0 = (double)(rad * c);
     z1 = (double)(rad * s);
   }
+  __device__ __forceinline__ void normal2f(uint32_t a, uint32_t b, float& z0, float& z1) {
+    const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
+    const float u2 = (float)b * 2.3283064365386963e-10f;
+    const float rad = sqrtf(-2.0f * logf(u1));
+    float s, c;
+    sincospif(2.0f * u2, &s, &c);
+    z0 = rad * c;
+    z1 = rad * s;
+  }
   // uniform in [0, 1) with 53 random bits
   __device__ __forceinline__ double uniform53(uint32_t hi, uint32_t lo) {
     return ((double)(hi >> 5) * 67108864.0 + (double)(lo >> 6)) * 1.1102230246251565e-16;
@@ -63,7 +72,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
                                                           unsigned char* __restrict__ scr, int64_t ss,
                                                           const EPShape S) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables<R> t = load_tables<R>(d, d.nmo_used, smem + S.o_tab);
+  const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
   const int64_t nw = a.nwalkers;
   const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne;
   const int64_t w0 = (int64_t)blockIdx.x * nwb;
@@ -71,15 +80,15 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
   const int e = tid / nwb, wl = tid - (tid / nwb) * nwb;
   const int64_t w = w0 + wl;
   const bool live = e < ne && w < nw;  // electron thread of a real walker
-  double* P = reinterpret_cast<double*>(smem + S.o_pos);    // current positions
-  double* PN = reinterpret_cast<double*>(smem + S.o_pnew);  // proposal
+  XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);    // current positions
+  XP<R>* PN = reinterpret_cast<XP<R>*>(smem + S.o_pnew);  // proposal
   double* PSI = reinterpret_cast<double*>(smem + S.o_psi);
   double* F = reinterpret_cast<double*>(smem + S.o_f);
   int* IEL = reinterpret_cast<int*>(smem + S.o_iel);
   int* ACC = reinterpret_cast<int*>(smem + S.o_acc);
   const EPPtrs ptrs{smem, S};
   const double eps = 1e-16;
-  ep_stage_positions(a.pos, w0, nw, nwb, nc, P);
+  ep_stage_positions<R>(a.pos, w0, nw, nwb, nc, P);
   ep_eval<R, JC, false>(d, t, ptrs, P, scr, ss, w0, nw);
   int nacc = 0;
   double psi_cur = 0.0;  // combine threads: psi at the current positions
@@ -115,43 +124,39 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
         __syncthreads();
       }
       // proposal
-      if (live) {
-        const bool moves = a.move_type == QMC_MOVE_ALL_ELEC ||
-                           (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]);
-        double z[3] = {0.0, 0.0, 0.0};
-        if (moves) {
-          if (a.proposals) {
-            if (a.move_type == QMC_MOVE_ALL_ELEC) {
-              const double* pr = a.proposals + ((int64_t)istep * nw + w) * nc + 3 * e;
-              z[0] = pr[0];
-              z[1] = pr[1];
-              z[2] = pr[2];
-            } else {
-              const double* pr = a.proposals + (((int64_t)istep * nmove + im) * nw + w) * 3;
-              z[0] = pr[0];
-              z[1] = pr[1];
-              z[2] = pr[2];
-            }
-          } else {
-            rng.call = call0 + e;
-            const U4 r = rng.next();
-            if (a.proba == QMC_PROBA_NORMAL) {
-              double z3;
-              rng.normal2(r.x, r.y, z[0], z[1]);
-              rng.normal2(r.z, r.w, z[2], z3);
-              z[0] *= sd;
-              z[1] *= sd;
-              z[2] *= sd;
-            } else {
-              const uint32_t rr[3] = {r.x, r.y, r.z};
-              for (int q = 0; q < 3; ++q)
-                z[q] = a.step_size * (2.0 * (rr[q] * 2.3283064365386963e-10) - 1.0);
-            }
+      if (e < ne) {
+        const bool moves = live && (a.move_type == QMC_MOVE_ALL_ELEC ||
+                                    (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]));
+        XP<R>* pn = PN + wl * nc + 3 * e;
+        const XP<R>* pc = P + wl * nc + 3 * e;
+        if (moves && a.proposals) {
+          const double* pr = a.move_type == QMC_MOVE_ALL_ELEC
+                                 ? a.proposals + ((int64_t)istep * nw + w) * nc + 3 * e
+                                 : a.proposals + (((int64_t)istep * nmove + im) * nw + w) * 3;
+          for (int q = 0; q < 3; ++q) {
+            const R zh = (R)pr[q];
+            pn[q] = xp_add<R>(pc[q], zh, (R)(pr[q] - (double)zh));
           }
+        } else if (moves) {
+          rng.call = call0 + e;
+          const U4 r = rng.next();
+          R z[3];
+          if (a.proba == QMC_PROBA_NORMAL) {
+            float f0, f1, f2, f3;
+            rng.normal2f(r.x, r.y, f0, f1);
+            rng.normal2f(r.z, r.w, f2, f3);
+            z[0] = (R)f0 * (R)sd;
+            z[1] = (R)f1 * (R)sd;
+            z[2] = (R)f2 * (R)sd;
+          } else {
+            const uint32_t rr[3] = {r.x, r.y, r.z};
+            for (int q = 0; q < 3; ++q)
+              z[q] = (R)a.step_size * ((R)2 * ((R)rr[q] * (R)2.3283064365386963e-10) - (R)1);
+          }
+          for (int q = 0; q < 3; ++q) pn[q] = xp_add<R>(pc[q], z[q]);
+        } else {
+          for (int q = 0; q < 3; ++q) pn[q] = pc[q];
         }
-        for (int q = 0; q < 3; ++q) PN[wl * nc + 3 * e + q] = P[wl * nc + 3 * e + q] + z[q];
-      } else if (e < ne) {
-        for (int q = 0; q < 3; ++q) PN[wl * nc + 3 * e + q] = P[wl * nc + 3 * e + q];
       }
       __syncthreads();
       ep_eval<R, JC, false>(d, t, ptrs, PN, scr, ss, w0, nw);
@@ -188,7 +193,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
       if (idecor % a.ndecor == 0) {
         if (a.samples && isnap < a.nsnap && live) {
           double* out = a.samples + (isnap * nw + w) * nc + 3 * e;
-          for (int q = 0; q < 3; ++q) out[q] = P[wl * nc + 3 * e + q];
+          for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * nc + 3 * e + q]);
         }
         ++isnap;
       }
@@ -196,7 +201,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
     }
   }
   if (live)
-    for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = P[wl * nc + 3 * e + q];
+    for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * nc + 3 * e + q]);
   if (tid < nwb && w0 + tid < nw) {
     if (a.accepted) a.accepted[w0 + tid] += nacc;
     if (a.psi_out) a.psi_out[w0 + tid] = psi_cur;
@@ -206,7 +211,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
 template <typename R, int JC>
 static int launch_metropolis(const qmc_wf_desc* d, const qmc_metropolis_args* a, unsigned char* scr,
                              cudaStream_t s) {
-  const EPShape S = ep_choose<R>(*d, 2);
+  const EPShape S = ep_choose<R>(*d, 2, JC);
   if (S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
   int st = prepare_smem(metropolis_kernel<R, JC>, S.smem);
   if (st) return st;

@@ -13,7 +13,7 @@ __global__ void __launch_bounds__(128) ao_kernel(const qmc_wf_desc d, const doub
                                                  int64_t nw, int mode, double* __restrict__ ao,
                                                  double* __restrict__ dao, double* __restrict__ d2ao) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables<double> t = load_tables<double>(d, 0, smem);
+  const Tables<double> t = load_tables<double>(d, 0, 0, smem);
   const int64_t item = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;  // (walker, electron)
   if (item >= nw * d.nelec) return;
   const double* pe = pos + item * 3;  // pos[w][3*ne] row-major == [(w*ne+e)*3]
@@ -43,7 +43,7 @@ __global__ void __launch_bounds__(128) ao_kernel(const qmc_wf_desc d, const doub
 __global__ void __launch_bounds__(128) mo_kernel(const qmc_wf_desc d, const double* __restrict__ ao,
                                                  int64_t nrows, double* __restrict__ mo) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables<double> t = load_tables<double>(d, d.nmo, smem);
+  const Tables<double> t = load_tables<double>(d, d.nmo, round_up(d.nmo, 8), smem);
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows) return;
   const double* ar = ao + r * d.nao;
@@ -54,7 +54,7 @@ __global__ void __launch_bounds__(128) mo_kernel(const qmc_wf_desc d, const doub
     for (int jj = 0; jj < JC; ++jj) acc[jj] = 0.0;
     for (int a = 0; a < d.nao; ++a) {
       const double v = ar[a];
-      const double* Wa = t.W + (int64_t)a * d.nmo + j0;
+      const double* Wa = t.W + (int64_t)a * t.ncol + j0;
 #pragma unroll
       for (int jj = 0; jj < JC; ++jj)
         if (j0 + jj < d.nmo) acc[jj] = fma(v, Wa[jj], acc[jj]);
@@ -119,14 +119,21 @@ __global__ void __launch_bounds__(kTPB) slater_kernel(const qmc_wf_desc d, const
   const int ne = d.nelec;
   const CView<double> m{mo + w * ne * ld, ld, 1};
   const CView<double> b = OP ? CView<double>{bop + w * ne * ld, ld, 1} : m;
-  const SpinWork<double> wk = spin_work<double>(L, scr, ss, w);
+  const int64_t vm = L.vmax > 0 ? L.vmax : 1;
+  SpinWork<double> wk;
+  wk.LU = MView<double>{rptr<double>(scr, L.lu, ss, w), (int64_t)L.nmax * ss, ss};
+  wk.X = MView<double>{rptr<double>(scr, L.x, ss, w), vm * ss, ss};
+  wk.Y = MView<double>{rptr<double>(scr, L.y, ss, w), (int64_t)L.omax * ss, ss};
+  wk.rc = wk.LU;  // unused: FP64 needs no refinement
+  wk.X64 = wk.X;
+  wk.Y64 = wk.Y;
   double* dv = rptr<double>(scr, L.dv, ss, w);
   double* ov = rptr<double>(scr, L.ov, ss, w);
   double dref[2];
-  spin_channel<double, OP>(d, 0, m, b, wk, SpinOut{dv, ov, ss, &dref[0]});
+  spin_channel<double, OP>(d, 0, m, b, wk, SpinOut<double>{dv, ov, ss, &dref[0]});
   spin_channel<double, OP>(d, 1, CView<double>{m.p + d.nup * m.rs, m.rs, m.cs},
                            CView<double>{b.p + d.nup * b.rs, b.rs, b.cs}, wk,
-                           SpinOut{dv + d.ndet[0] * ss, ov + d.ndet[0] * ss, ss, &dref[1]});
+                           SpinOut<double>{dv + d.ndet[0] * ss, ov + d.ndet[0] * ss, ss, &dref[1]});
   for (int k = 0; k < d.ncfg; ++k) {
     const int iu = __ldg(d.cfg_det[0] + k), idn = __ldg(d.cfg_det[1] + k) + d.ndet[0];
     dets[w * d.ncfg + k] = (dref[0] * dv[iu * ss]) * (dref[1] * dv[idn * ss]);
@@ -192,7 +199,7 @@ int qmc_mo_eval(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* m
   if (st) return st;
   if (nrows < 0 || (nrows > 0 && (!ao || !mo))) return QMC_ERR_ARG;
   if (nrows == 0) return QMC_OK;
-  const int64_t smem = tables_smem_bytes<double>(*d, d->nmo);
+  const int64_t smem = tables_smem_bytes<double>(*d, round_up(d->nmo, 8));
   if ((st = prepare_smem(mo_kernel, smem))) return st;
   mo_kernel<<<(unsigned)((nrows + 127) / 128), 128, smem, (cudaStream_t)stream>>>(*d, ao, nrows, mo);
   return launch_status();

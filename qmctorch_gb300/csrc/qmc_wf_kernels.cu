@@ -18,10 +18,10 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_psi_kernel(const qmc_
                                                       unsigned char* __restrict__ scr, int64_t ss,
                                                       const EPShape S) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables<R> t = load_tables<R>(d, d.nmo_used, smem + S.o_tab);
+  const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
   const int64_t w0 = (int64_t)blockIdx.x * S.nwb;
-  double* P = reinterpret_cast<double*>(smem + S.o_pos);
-  ep_stage_positions(pos, w0, nw, S.nwb, 3 * d.nelec, P);
+  XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);
+  ep_stage_positions<R>(pos, w0, nw, S.nwb, 3 * d.nelec, P);
   ep_eval<R, JC, false>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
   const int tid = threadIdx.x;
   if (tid < S.nwb && w0 + tid < nw)
@@ -36,10 +36,10 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_eloc_kernel(const qmc
                                                        unsigned char* __restrict__ scr, int64_t ss,
                                                        const EPShape S) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const Tables<R> t = load_tables<R>(d, d.nmo_used, smem + S.o_tab);
+  const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
   const int64_t w0 = (int64_t)blockIdx.x * S.nwb;
-  double* P = reinterpret_cast<double*>(smem + S.o_pos);
-  ep_stage_positions(pos, w0, nw, S.nwb, 3 * d.nelec, P);
+  XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);
+  ep_stage_positions<R>(pos, w0, nw, S.nwb, 3 * d.nelec, P);
   ep_eval<R, JC, true>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
   const int tid = threadIdx.x;
   if (tid < S.nwb && w0 + tid < nw) {
@@ -60,7 +60,7 @@ static int launch_prepare(K kernel, const EPShape& S) {
 template <typename R, int JC>
 static int launch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, double* psi,
                       unsigned char* scr, cudaStream_t s) {
-  const EPShape S = ep_choose<R>(*d, 0);
+  const EPShape S = ep_choose<R>(*d, 0, JC);
   int st = launch_prepare<R>(ep_psi_kernel<R, JC>, S);
   if (st) return st;
   const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
@@ -79,7 +79,7 @@ static int dispatch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, dou
 template <typename R, int JC>
 static int launch_eloc(const qmc_wf_desc* d, const double* pos, int64_t nw, double* eloc,
                        double* kin, double* psi, unsigned char* scr, cudaStream_t s) {
-  const EPShape S = ep_choose<R>(*d, 1);
+  const EPShape S = ep_choose<R>(*d, 1, JC);
   int st = launch_prepare<R>(ep_eloc_kernel<R, JC>, S);
   if (st) return st;
   const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
