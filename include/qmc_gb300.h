@@ -90,6 +90,8 @@ typedef struct qmc_wf_desc {
   const double* bas_exp;      /* [nentries] trainable exponents (ao.bas_exp) */
   const int32_t* ao_k;        /* [nao*3] cartesian powers kx, ky, kz */
   const int32_t* ao_wofs;     /* [nao] offset of the AO's weights (one per group primitive) */
+  const int32_t* weight_entry;/* [nweight] basis entry (bas_exp index) of each AO weight; a group
+                                 whose components' exponents differ is evaluated per component */
   const double* ao_wd;        /* [nweight] bas_coeffs * norm (derivative / contracted path) */
   const double* ao_wv;        /* [nweight] weights of the value path when contract == 0, else NULL */
   const double* mo_scf;       /* [nao*nmo] */
@@ -198,6 +200,27 @@ int qmc_slater(const qmc_wf_desc* d, const double* mo, const double* bop, int32_
  */
 int qmc_potentials(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double* v_en,
                    double* v_ee, void* stream);
+
+/* Scratch bytes for qmc_wf_psi_adjoint. */
+int64_t qmc_adjoint_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
+
+/*
+ * Adjoint of psi (FP64, AO values recomputed, not stored): accumulates
+ *   grad_exp[e]      += sum_w gout[w] d psi_w / d bas_exp[e]   (e < nentries)
+ *   grad_W[a*ldw+j]  += sum_w gout[w] d psi_w / d W[a][j]      (j < nmo_used,
+ *                       W = mo_scf * mo_modifier; d/d mo_modifier = this * mo_scf)
+ *   grad_jastrow_w[0]+= sum_w gout[w] d psi_w / d w            (if use_jastrow)
+ *   grad_ci[k]       += sum_w gout[w] d psi_w / d c_k
+ * weight_entry[i] maps AO weight i (ao_wd index) to its basis entry. The outputs
+ * are accumulated (zero them first); the summation order over walkers is not
+ * fixed (atomic adds). Replaces the autograd backward of SlaterJastrow.forward
+ * that Solver.evaluate_grad_manual runs with psi.backward(weight)
+ * (solver.py:372-431).
+ */
+int qmc_wf_psi_adjoint(const qmc_wf_desc* d, const double* pos, int64_t nwalkers,
+                       const double* gout, const int32_t* weight_entry, int32_t nentries,
+                       double* grad_exp, double* grad_W, int32_t ldw, double* grad_jastrow_w,
+                       double* grad_ci, void* scratch, int64_t scratch_bytes, void* stream);
 
 /* Metropolis move types (Metropolis.configure_move, metropolis.py:179-225). */
 #define QMC_MOVE_ALL_ELEC 0

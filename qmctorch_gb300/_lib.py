@@ -23,7 +23,7 @@ BUILD = os.path.join(ROOT, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
-           "qmc_probe.cu"]
+           "qmc_probe.cu", "qmc_adjoint.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 
@@ -87,7 +87,8 @@ class WfDesc(ctypes.Structure):
         ("use_jastrow", c_int32), ("precision", c_int32),
         ("atom_coords", c_void_p), ("atom_charge", c_void_p), ("group_atom", c_void_p),
         ("group_prim", c_void_p), ("group_ao", c_void_p), ("gprim_entry", c_void_p),
-        ("bas_exp", c_void_p), ("ao_k", c_void_p), ("ao_wofs", c_void_p), ("ao_wd", c_void_p),
+        ("bas_exp", c_void_p), ("ao_k", c_void_p), ("ao_wofs", c_void_p), ("weight_entry", c_void_p),
+        ("ao_wd", c_void_p),
         ("ao_wv", c_void_p), ("mo_scf", c_void_p), ("mo_modifier", c_void_p),
         ("jastrow_w", c_void_p),
         ("det_mode", c_int32), ("ncfg", c_int32), ("max_orb", c_int32 * 2),
@@ -128,6 +129,10 @@ SIGNATURES = {
                                   c_void_p, c_void_p, c_int64, c_void_p]),
     "qmc_potentials": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                       c_void_p]),
+    "qmc_adjoint_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
+    "qmc_wf_psi_adjoint": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
+                                          c_int32, c_void_p, c_void_p, c_int32, c_void_p,
+                                          c_void_p, c_void_p, c_int64, c_void_p]),
     "qmc_probe_fma": (ctypes.c_int, [c_int32, c_int32, c_int64, c_void_p, c_void_p]),
     "qmc_metropolis_run": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), c_void_p, c_int64,
                                           c_void_p]),

@@ -152,17 +152,35 @@ __device__ __forceinline__ void group_radial(const Tables<R>& t, int g, R r2, R 
   const int wb = t.ao_wofs[t.group_ao[g]];  // weights of component c at wb + c * np
 #pragma unroll
   for (int c = 0; c < NC; ++c) G0[c] = G1[c] = G2[c] = (R)0;
-  for (int p = 0; p < np; ++p) {
-    const R al = t.alpha[p0 + p];
-    const R e0 = rexp(-al * r2);
-    const R e1 = al * e0, e2 = al * e1;
+  if (!t.group_split[g]) {
+    for (int p = 0; p < np; ++p) {
+      const R al = t.alpha[p0 + p];
+      const R e0 = rexp(-al * r2);
+      const R e1 = al * e0, e2 = al * e1;
 #pragma unroll
-    for (int c = 0; c < NC; ++c) {
-      const R w = t.wd[wb + c * np + p];
-      G0[c] = fma(w, e0, G0[c]);
-      if (DERIV) {
-        G1[c] = fma(w, e1, G1[c]);
-        G2[c] = fma(w, e2, G2[c]);
+      for (int c = 0; c < NC; ++c) {
+        const R w = t.wd[wb + c * np + p];
+        G0[c] = fma(w, e0, G0[c]);
+        if (DERIV) {
+          G1[c] = fma(w, e1, G1[c]);
+          G2[c] = fma(w, e2, G2[c]);
+        }
+      }
+    }
+  } else {
+    // components with their own exponents
+    for (int p = 0; p < np; ++p) {
+#pragma unroll
+      for (int c = 0; c < NC; ++c) {
+        const int wi = wb + c * np + p;
+        const R al = t.walpha[wi];
+        const R e0 = rexp(-al * r2);
+        const R w = t.wd[wi];
+        G0[c] = fma(w, e0, G0[c]);
+        if (DERIV) {
+          G1[c] = fma(w, al * e0, G1[c]);
+          G2[c] = fma(w, al * al * e0, G2[c]);
+        }
       }
     }
   }

@@ -21,7 +21,7 @@ static inline int check_desc(const qmc_wf_desc* d) {
   if (d->nelec != d->nup + d->ndown || d->nup < 0 || d->ndown < 0) return QMC_ERR_ARG;
   if (d->nup > QMC_MAX_NSPIN || d->ndown > QMC_MAX_NSPIN) return QMC_ERR_SHAPE;
   if (!d->atom_coords || !d->atom_charge || !d->group_atom || !d->group_prim || !d->group_ao ||
-      !d->gprim_entry || !d->bas_exp || !d->ao_k || !d->ao_wofs || !d->ao_wd || !d->mo_scf ||
+      !d->gprim_entry || !d->bas_exp || !d->ao_k || !d->ao_wofs || !d->weight_entry || !d->ao_wd || !d->mo_scf ||
       !d->mo_modifier || !d->ci_weight || !d->cfg_det[0] || !d->cfg_det[1])
     return QMC_ERR_ARG;
   if (!d->contract && !d->ao_wv) return QMC_ERR_ARG;

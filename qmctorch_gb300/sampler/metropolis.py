@@ -93,7 +93,8 @@ class Walkers:
                     s = 2.0 / (self.init_domain["atom_num"][i] - 2)
                 else:
                     s = 3.0 / (self.init_domain["atom_num"][i] - 3)
-                xyz[ie, :] += np.random.normal(scale=s, size=(1, 3))
+                xyz[ie, :] += torch.as_tensor(np.random.normal(scale=s, size=(1, 3)),
+                                              dtype=xyz.dtype).reshape(3)
                 placed[i] += 1
             pos[iw, :] = xyz.view(-1)
         return pos.to(device=self.device)

@@ -69,6 +69,28 @@ class WaveFunction(nn.Module):
 PRECISIONS = {"fp64": 0, "mixed": 1}
 
 
+class _PsiFunction(torch.autograd.Function):
+    """psi with a hand-written adjoint (``qmc_wf_psi_adjoint``) for the
+    trainable parameters; AO values are recomputed in the backward pass.
+    Gradients with respect to the electron positions are not provided."""
+
+    @staticmethod
+    def forward(ctx, x, bas_exp, mo_modifier, jastrow_w, fc_weight, wf):
+        ctx.wf = wf
+        xd = rt.dev64(x, rt.cuda_device()).reshape(-1, wf.ndim_tot)
+        ctx.save_for_backward(xd)
+        return wf._psi(xd).reshape(-1, 1).to(device=x.device, dtype=x.dtype)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (xd,) = ctx.saved_tensors
+        wf = ctx.wf
+        g_exp, g_mod, g_w, g_fc = wf._psi_adjoint(xd, gout.reshape(-1))
+        need = ctx.needs_input_grad
+        return (None, g_exp if need[1] else None, g_mod if need[2] else None,
+                g_w if need[3] else None, g_fc if need[4] else None, None)
+
+
 class SlaterJastrow(WaveFunction):
     """``precision`` (keyword added to the reference signature) selects the
     arithmetic of the fused psi / local-energy / Metropolis kernels: "fp64"
@@ -133,6 +155,7 @@ class SlaterJastrow(WaveFunction):
         self.gradients = self.gradients_jacobi
         self.kinetic_energy = self.kinetic_energy_jacobi
         self._enuc_cache = (None, 0.0)
+        self._no_jastrow_w = torch.zeros(1)
         if cuda:
             self.device = rt.cuda_device()
             self.to(self.device)
@@ -186,13 +209,45 @@ class SlaterJastrow(WaveFunction):
         return el, kin
 
     def forward(self, x, ao=None):
-        """psi = J * sum_n c_n D_up D_down -> (nbatch, 1) (slater_jastrow.py:243-286)."""
+        """psi = J * sum_n c_n D_up D_down -> (nbatch, 1) (slater_jastrow.py:243-286).
+        Differentiable with respect to ao.bas_exp, mo.mo_modifier,
+        jastrow.jastrow_kernel.weight and fc.weight (hand-written adjoint)."""
         if ao is not None:
             out = self.fc(self.pool(self.mo(ao)))
             if self.use_jastrow:
                 out = self.jastrow(x) * out
             return out
+        jw = self.jastrow.jastrow_kernel.weight if self.use_jastrow else self._no_jastrow_w
+        params = (self.ao.bas_exp, self.mo.mo_modifier, jw, self.fc.weight)
+        if torch.is_grad_enabled() and any(p.requires_grad for p in params):
+            return _PsiFunction.apply(x, *params, self)
         return self._psi(x).reshape(-1, 1).to(device=x.device, dtype=x.dtype)
+
+    def _psi_adjoint(self, x, gout):
+        """Parameter gradients of sum_w gout[w] psi_w (qmc_wf_psi_adjoint)."""
+        device = rt.cuda_device()
+        nb = x.shape[0]
+        call = self._desc(device)
+        bt = self.ao.device_tables(device)
+        nmu = self.highest_occ_mo
+        lib = _lib.lib()
+        g = rt.dev64(gout, device)
+        g_exp = torch.zeros(bt.nentries, dtype=rt.F64, device=device)
+        g_W = torch.zeros((self.ao.norb, nmu), dtype=rt.F64, device=device)
+        g_w = torch.zeros(1, dtype=rt.F64, device=device)
+        g_ci = torch.zeros(self.nci, dtype=rt.F64, device=device)
+        scr = rt.scratch(lib.qmc_adjoint_scratch_bytes(call.ref, nb), device)
+        _lib.check(lib.qmc_wf_psi_adjoint(call.ref, rt.ptr(x), nb, rt.ptr(g), rt.ptr(bt.t["w_entry"]),
+                                          bt.nentries, rt.ptr(g_exp), rt.ptr(g_W), nmu,
+                                          rt.ptr(g_w), rt.ptr(g_ci), rt.ptr(scr), scr.numel(),
+                                          rt.stream_handle()), "qmc_wf_psi_adjoint")
+        mod = self.mo.mo_modifier
+        g_mod = torch.zeros(mod.shape, dtype=rt.F64, device=device)
+        g_mod[:, :nmu] = g_W * rt.dev64(self.mo.mo_scf, device)[:, :nmu]
+        cast = lambda t, p: t.to(device=p.device, dtype=p.dtype).reshape(p.shape)  # noqa: E731
+        jw = self.jastrow.jastrow_kernel.weight if self.use_jastrow else self._no_jastrow_w
+        return (cast(g_exp, self.ao.bas_exp), cast(g_mod, mod), cast(g_w, jw),
+                cast(g_ci, self.fc.weight))
 
     def pdf(self, pos, return_grad=False):
         """psi^2 -> (nbatch,) (wf_base.py:241-247)."""

@@ -85,7 +85,7 @@ class BasisTables:
             a = b
         group_atom, group_prim, group_ao, gprim_entry = [], [0], [0], []
         ao_wofs = np.zeros(self.nao, dtype=np.int64)
-        wd, wv = [], []
+        wd, wv, w_entry = [], [], []
         for (a0, a1) in groups:
             ents0 = ao_entries[a0]
             group_atom.append(int(ao_atom[a0]))
@@ -97,6 +97,7 @@ class BasisTables:
                 for e in ao_entries[a]:
                     wd.append(coeffs[e] * norm[e])
                     wv.append(norm[e])
+                    w_entry.append(e)
         self.group_key = [exps[ao_entries[a0]].tobytes() for (a0, _) in groups]
         self.groups = groups
         self.ao_entries = ao_entries
@@ -106,11 +107,12 @@ class BasisTables:
             "group_atom": i32(group_atom), "group_prim": i32(group_prim),
             "group_ao": i32(group_ao), "gprim_entry": i32(gprim_entry),
             "ao_k": i32(ao_k.reshape(-1)), "ao_wofs": i32(ao_wofs), "ao_wd": f64(wd),
-            "ao_wv": f64(wv),
+            "ao_wv": f64(wv), "w_entry": i32(w_entry),
         }
         self.ngroup = len(groups)
         self.ngprim = len(gprim_entry)
         self.nweight = len(wd)
+        self.nentries = len(index_ctr)
 
     def still_valid(self, bas_exp_values):
         """True while every AO of a group keeps the group's exponents."""

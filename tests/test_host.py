@@ -76,6 +76,7 @@ def _desc_for(name):
     for f in ("group_atom", "group_prim", "group_ao", "gprim_entry", "ao_k", "ao_wofs"):
         setattr(desc, f, p(bt.t[f]))
     desc.ao_wd = p(bt.t["ao_wd"])
+    desc.weight_entry = p(bt.t["w_entry"])
     desc.det_mode = int(ct.explicit)
     desc.ncfg = ct.ncfg
     desc.max_orb[0], desc.max_orb[1] = ct.max_orb
