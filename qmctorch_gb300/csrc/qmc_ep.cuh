@@ -28,6 +28,7 @@ namespace qmc {
 // ---------------------------------------------------------------------------
 struct EPShape {
   int nwb;       // walkers per block
+  int nslot;     // threads per walker in the electron phase (electron e on slot e % nslot)
   int nthreads;  // threads per block
   int ncol;      // W columns stored per AO (nmo_used rounded up to the MO chunk)
   int64_t smem;  // dynamic shared memory bytes
@@ -36,10 +37,12 @@ struct EPShape {
 };
 
 template <typename R>
-__host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb, int jc) {
+__host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb, int jc,
+                                           int nslot) {
   EPShape s;
   s.nwb = nwb;
-  int nt = nwb * d.nelec;
+  s.nslot = nslot;
+  int nt = nwb * nslot;
   if (nt < 2 * nwb) nt = 2 * nwb;
   s.nthreads = ((nt + 31) / 32) * 32;
   s.ncol = round_up(d.nmo_used, jc);
@@ -85,16 +88,6 @@ template <typename R>
 struct EPBound {
   static constexpr int kThreads = kMixed<R> ? 1024 : 512;
 };
-
-// Largest walkers-per-block that fits the shared memory and the thread bound.
-template <typename R>
-__host__ inline EPShape ep_choose(const qmc_wf_desc& d, int kind, int jc) {
-  for (int nwb = 32; nwb > 1; nwb /= 2) {
-    const EPShape s = ep_shape<R>(d, kind, nwb, jc);
-    if (s.nthreads <= EPBound<R>::kThreads && s.smem <= 200 * 1024) return s;
-  }
-  return ep_shape<R>(d, kind, 1, jc);
-}
 
 // Per-walker scratch: the determinant-phase work arrays of both spins. The
 // relative determinant values are FP64 for the local energy and of the
@@ -482,8 +475,8 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   double* KINV = reinterpret_cast<double*>(p.smem + S.o_kin);
   double* V = reinterpret_cast<double*>(p.smem + S.o_v);
   {
-    const int e = tid / nwb, wl = tid - (tid / nwb) * nwb;
-    if (e < ne)
+    const int slot = tid / nwb, wl = tid - (tid / nwb) * nwb;
+    for (int e = slot; e < ne && slot < S.nslot; e += S.nslot)
       ep_electron<R, JC, KIN>(d, t, pbuf + wl * nc, e, MO + wl, BK + wl, nwb, &JR[e * nwb + wl],
                               &VR[e * nwb + wl]);
   }

@@ -4,6 +4,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "qmc_device.cuh"
 #include "qmc_ep.cuh"
 
@@ -60,6 +64,88 @@ static inline int64_t scratch_slot_bytes(const qmc_wf_desc* d, int kind) {
     if (t > b) b = t;
   }
   return b;
+}
+
+// Launch plan of an electron-parallel kernel for nw walkers: walkers per
+// block (nwb) and threads per walker (nslot; a thread evaluates electrons
+// slot, slot + nslot, ...).
+//
+// Rule, from sweeps of both on GB300 (H2O cc-pVDZ, 16384 walkers):
+// * nwb starts at 32 for FP32 and 16 for FP64 (FP64 threads hold twice the
+//   registers, so smaller blocks fill the register file in finer steps) and
+//   halves while the blocks would not cover the SMs, or the block does not
+//   fit the thread bound or 200 KB of shared memory.
+// * nslot = ceil(nelec / k) for the smallest k = 1..8 with which every block
+//   of the grid is resident at once (CUDA occupancy calculator). The
+//   Metropolis kernel is persistent over its steps, so a partial second wave
+//   would run alone at the end; fewer slots also give the determinant phase
+//   (two threads per walker) a larger share of the block. If no k gives one
+//   wave, the k with the best last-wave fill is taken.
+// * The FP64 local-energy kernel (heaviest electron phase: AO Hessian
+//   diagonals in FP64) keeps one thread per electron (k = 1).
+// Plans are cached per (kernel, device, walker count, shape inputs).
+template <typename R, typename K>
+static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, int64_t nw) {
+  int dev = 0, nsm = 1;
+  cudaGetDevice(&dev);
+  const int ne = d.nelec > 0 ? d.nelec : 1;
+  const EPShape s1 = ep_shape<R>(d, kind, 1, jc, ne), s2 = ep_shape<R>(d, kind, 2, jc, ne);
+  struct Key {
+    const void* kernel;
+    int dev, kind, jc, ne;
+    int64_t nw, smem1, smem2;
+    bool operator==(const Key& o) const {
+      return kernel == o.kernel && dev == o.dev && kind == o.kind && jc == o.jc && ne == o.ne &&
+             nw == o.nw && smem1 == o.smem1 && smem2 == o.smem2;
+    }
+  };
+  const Key key{(const void*)kernel, dev, kind, jc, ne, nw, s1.smem, s2.smem};
+  static std::mutex mu;
+  static std::vector<std::pair<Key, EPShape>> cache;
+  {
+    std::lock_guard<std::mutex> g(mu);
+    for (const auto& kv : cache)
+      if (kv.first == key) return kv.second;
+  }
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  int nwb = kMixed<R> ? 32 : 16;
+  while (nwb > 8 && (nw + nwb - 1) / nwb < nsm) nwb /= 2;
+  const int kmax = (kind == 1 && !kMixed<R>) ? 1 : 8;
+  EPShape best = s1;
+  best.smem = -1;  // nothing fits yet
+  for (; nwb >= 1 && best.smem < 0; nwb /= 2) {
+    double best_fill = -1.0;
+    for (int k = 1; k <= kmax; ++k) {
+      const int nslot = (ne + k - 1) / k;
+      if (k > 1 && nslot == (ne + k - 2) / (k - 1)) continue;  // same slot count as k - 1
+      const EPShape s = ep_shape<R>(d, kind, nwb, jc, nslot);
+      if (s.nthreads > EPBound<R>::kThreads || s.smem > 200 * 1024) continue;
+      if (prepare_smem(kernel, s.smem) != QMC_OK) continue;
+      int occ = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, s.nthreads, s.smem) !=
+              cudaSuccess ||
+          occ < 1) {
+        cudaGetLastError();
+        continue;
+      }
+      const int64_t blocks = (nw + nwb - 1) / nwb, slots = (int64_t)occ * nsm;
+      if (blocks <= slots) {  // one wave
+        best = s;
+        break;
+      }
+      const double fill = (double)blocks / (double)(((blocks + slots - 1) / slots) * slots);
+      if (fill > best_fill) {
+        best = s;
+        best_fill = fill;
+      }
+    }
+  }
+  if (best.smem >= 0) {
+    std::lock_guard<std::mutex> g(mu);
+    if (cache.size() > 256) cache.clear();
+    cache.emplace_back(key, best);
+  }
+  return best;
 }
 
 }  // namespace qmc

@@ -77,9 +77,11 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
   const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne;
   const int64_t w0 = (int64_t)blockIdx.x * nwb;
   const int tid = threadIdx.x;
-  const int e = tid / nwb, wl = tid - (tid / nwb) * nwb;
+  const int slot = tid / nwb, wl = tid - (tid / nwb) * nwb;
+  const int nslot = S.nslot;
   const int64_t w = w0 + wl;
-  const bool live = e < ne && w < nw;  // electron thread of a real walker
+  const bool active = slot < nslot;    // an electron slot (electrons slot, slot + nslot, ...)
+  const bool live = active && w < nw;  // ... of a real walker
   XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);    // current positions
   XP<R>* PN = reinterpret_cast<XP<R>*>(smem + S.o_pnew);  // proposal
   double* PSI = reinterpret_cast<double*>(smem + S.o_psi);
@@ -124,7 +126,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
         __syncthreads();
       }
       // proposal
-      if (e < ne) {
+      for (int e = slot; e < ne && active; e += nslot) {
         const bool moves = live && (a.move_type == QMC_MOVE_ALL_ELEC ||
                                     (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]));
         XP<R>* pn = PN + wl * nc + 3 * e;
@@ -186,22 +188,25 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
       }
       __syncthreads();
       if (live && ACC[wl])
-        for (int q = 0; q < 3; ++q) P[wl * nc + 3 * e + q] = PN[wl * nc + 3 * e + q];
+        for (int e = slot; e < ne; e += nslot)
+          for (int q = 0; q < 3; ++q) P[wl * nc + 3 * e + q] = PN[wl * nc + 3 * e + q];
       __syncthreads();
     }
     if (istep >= a.ntherm) {
       if (idecor % a.ndecor == 0) {
-        if (a.samples && isnap < a.nsnap && live) {
-          double* out = a.samples + (isnap * nw + w) * nc + 3 * e;
-          for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * nc + 3 * e + q]);
-        }
+        if (a.samples && isnap < a.nsnap && live)
+          for (int e = slot; e < ne; e += nslot) {
+            double* out = a.samples + (isnap * nw + w) * nc + 3 * e;
+            for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * nc + 3 * e + q]);
+          }
         ++isnap;
       }
       ++idecor;
     }
   }
   if (live)
-    for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * nc + 3 * e + q]);
+    for (int e = slot; e < ne; e += nslot)
+      for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * nc + 3 * e + q]);
   if (tid < nwb && w0 + tid < nw) {
     if (a.accepted) a.accepted[w0 + tid] += nacc;
     if (a.psi_out) a.psi_out[w0 + tid] = psi_cur;
@@ -211,8 +216,8 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
 template <typename R, int JC>
 static int launch_metropolis(const qmc_wf_desc* d, const qmc_metropolis_args* a, unsigned char* scr,
                              cudaStream_t s) {
-  const EPShape S = ep_choose<R>(*d, 2, JC);
-  if (S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
+  const EPShape S = ep_plan<R>(*d, 2, JC, metropolis_kernel<R, JC>, a->nwalkers);
+  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
   int st = prepare_smem(metropolis_kernel<R, JC>, S.smem);
   if (st) return st;
   const dim3 grid((unsigned)((a->nwalkers + S.nwb - 1) / S.nwb));

@@ -53,14 +53,14 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_eloc_kernel(const qmc
 
 template <typename R, typename K>
 static int launch_prepare(K kernel, const EPShape& S) {
-  if (S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
+  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
   return prepare_smem(kernel, S.smem);
 }
 
 template <typename R, int JC>
 static int launch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, double* psi,
                       unsigned char* scr, cudaStream_t s) {
-  const EPShape S = ep_choose<R>(*d, 0, JC);
+  const EPShape S = ep_plan<R>(*d, 0, JC, ep_psi_kernel<R, JC>, nw);
   int st = launch_prepare<R>(ep_psi_kernel<R, JC>, S);
   if (st) return st;
   const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
@@ -79,7 +79,7 @@ static int dispatch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, dou
 template <typename R, int JC>
 static int launch_eloc(const qmc_wf_desc* d, const double* pos, int64_t nw, double* eloc,
                        double* kin, double* psi, unsigned char* scr, cudaStream_t s) {
-  const EPShape S = ep_choose<R>(*d, 1, JC);
+  const EPShape S = ep_plan<R>(*d, 1, JC, ep_eloc_kernel<R, JC>, nw);
   int st = launch_prepare<R>(ep_eloc_kernel<R, JC>, S);
   if (st) return st;
   const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));

@@ -85,3 +85,29 @@ def test_mixed_metropolis_replay_decisions(name):
     out = sampler(wf.pdf, pos=torch.as_tensor(d["met_pos0"], device="cuda"), with_tqdm=False,
                   replay={"proposals": props, "uniforms": unif})
     np.testing.assert_allclose(out.detach().cpu().numpy(), d["met_out"], rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_size_does_not_change_results(precision):
+    """The launch plan (walkers per block, threads per walker) depends on the
+    batch size; each walker's arithmetic does not. psi, E_L and a Metropolis
+    chain of the first 64 walkers are bitwise the same alone and inside a
+    batch of 16384."""
+    from qmctorch_gb300.sampler import Metropolis
+    mol, d = load("h2o_sd")
+    wf = make_wf(mol, d, precision)
+    rng = np.random.default_rng(77)
+    centers = np.repeat(np.asarray(mol.atom_coords), mol.atomic_nelec, axis=0)
+    big = torch.as_tensor((centers[None] + rng.normal(size=(16384, 10, 3))).reshape(16384, -1),
+                          device="cuda")
+    small = big[:64].clone()
+    with torch.no_grad():
+        np.testing.assert_array_equal(wf(small).cpu().numpy(), wf(big)[:64].cpu().numpy())
+    np.testing.assert_array_equal(wf.local_energy(small).cpu().numpy(),
+                                  wf.local_energy(big)[:64].cpu().numpy())
+    outs = []
+    for x in (small, big):
+        s = Metropolis(nwalkers=len(x), nstep=30, step_size=0.2, nelec=10,
+                       init=mol.domain("atomic"), cuda=True, seed=9)
+        outs.append(s(wf.pdf, pos=x.clone(), with_tqdm=False)[:64].detach().cpu().numpy())
+    np.testing.assert_array_equal(outs[0], outs[1])
