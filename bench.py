@@ -36,6 +36,17 @@ H2O = "O 0 0 0.1173; H 0 0.7572 -0.4692; H 0 -0.7572 -0.4692"
 CONFIGS = "single_double(4,4)"
 STEP_SIZE = 0.2
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+NWALKERS = 16384
+METRIC = ("walker-steps/s (Metropolis all-electron, mixed-precision method; "
+          "E_L/s and the plain FP64 method alongside)")
+
+
+def workload_config(args, nw):
+    return {"workload": "h2o_ccpvdz_single_double44_16384w",
+            "molecule": "H2O cc-pVDZ (25 cart AOs, 10 e)", "configs": CONFIGS,
+            "nwalkers_per_gpu": nw, "mc_steps_per_step": args.mc_steps, "step_size": STEP_SIZE,
+            "method": "mixed (FP32 + FP64 refinement)",
+            "l2": "flushed between timed steps (256 MB write)"}
 
 
 def parse():
@@ -79,29 +90,32 @@ def _cpu_worker(args):
     return time.perf_counter() - t0, nw * nstep
 
 
-def cpu_baseline(target_seconds, steps=1):
+def cpu_baseline(target_seconds, steps=1, warmup=0):
     """Oracle Metropolis on the host cores: one spawn process per core, each
-    advancing its own bounded walker sample; returns walker-steps/s."""
+    advancing its own bounded walker sample. ``steps`` timed rounds (after
+    ``warmup`` untimed ones) of about ``target_seconds`` each; returns
+    walker-steps/s over the timed wall time and the wall time per round."""
     ncores = os.cpu_count() or 1
     ctx = mp.get_context("spawn")
-    # calibrate: one small chunk on one core
-    with ctx.Pool(1) as pool:
-        dt, n = pool.map(_cpu_worker, [(64, 2, 0)])[0]
-    rate1 = n / dt
-    per_core = max(32, int(rate1 * target_seconds / max(steps, 1) / 2))
     nstep = 2
-    nw = max(16, per_core // nstep)
-    results = []
-    t0 = time.perf_counter()
+    total, walls = 0, []
     with ctx.Pool(ncores) as pool:
-        for _ in range(steps):
-            results += pool.map(_cpu_worker, [(nw, nstep, 100 + i) for i in range(ncores)])
-    wall = time.perf_counter() - t0
-    total = sum(r[1] for r in results)
-    busy = max(r[0] for r in results) * steps
-    return {"value": total / busy, "unit": "walker-steps/s", "cores": ncores, "kind": "port",
-            "sample": "%d processes x %d walkers x %d all-electron steps (H2O cc-pVDZ "
-                      "single_double(4,4), numpy oracle), %.1f s wall" % (ncores, nw, nstep, wall)}
+        # calibrate: one small chunk per core, all cores busy
+        res = pool.map(_cpu_worker, [(64, 2, k) for k in range(ncores)])
+        rate1 = min(n / dt for dt, n in res)
+        nw = max(16, int(rate1 * target_seconds / 1.1) // nstep)
+        for i in range(warmup + steps):
+            t0 = time.perf_counter()
+            res = pool.map(_cpu_worker, [(nw, nstep, 100 + 37 * i + k) for k in range(ncores)])
+            if i >= warmup:
+                walls.append(time.perf_counter() - t0)
+                total += sum(r[1] for r in res)
+    wall = sum(walls)
+    return {"value": total / wall, "unit": "walker-steps/s", "cores": ncores, "kind": "port",
+            "ms_per_round": wall * 1e3 / len(walls),
+            "sample": "%d round(s) of %d processes x %d walkers x %d all-electron steps "
+                      "(H2O cc-pVDZ single_double(4,4), numpy oracle), %.1f s wall timed"
+                      % (len(walls), ncores, nw, nstep, wall)}
 
 
 # ----------------------------------------------------------------------------
@@ -158,7 +172,7 @@ def probe_peaks(torch, lib, device):
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     res = {}
     for kind, name, iters, per in ((0, "fp64_gflops", 2000, 16), (1, "fp32_gflops", 20000, 16),
-                                   (2, "fp32_exp_gps", 10000, 8), (3, "fp64_exp_gps", 500, 8)):
+                                   (2, "fp32_exp_gps", 10000, 8), (3, "fp64_exp_gps", 100, 8)):
         lib.qmc_probe_fma(kind, blocks, iters, ctypes.c_void_p(out.data_ptr()), stream)
         torch.cuda.synchronize()
         best = 0.0
@@ -348,8 +362,7 @@ def run_gb300(args):
         ach_m = flops * launch_units / (m_met / args.steps) / 1e9
         ach_f = flops * launch_units / (f_met / args.steps) / 1e9
         line = {
-            "metric": "walker-steps/s (Metropolis all-electron, mixed-precision method; "
-                      "E_L/s and the plain FP64 method alongside)",
+            "metric": METRIC,
             "value": value,
             "unit": "walker-steps/s",
             "n_gpus": world,
@@ -361,11 +374,7 @@ def run_gb300(args):
             "vs_baseline": None,
             "dtype": "f32+f64 (mixed)",
             "data": "synthetic (seeded walker positions; built-in cc-pVDZ tables, extended-Hueckel MOs)",
-            "config": {"workload": "h2o_ccpvdz_single_double44_16384w",
-                       "molecule": "H2O cc-pVDZ (25 cart AOs, 10 e)", "configs": CONFIGS,
-                       "nwalkers_per_gpu": nw, "mc_steps_per_step": args.mc_steps,
-                       "step_size": STEP_SIZE, "method": "mixed (FP32 + FP64 refinement)",
-                       "l2": "flushed between timed steps (256 MB write)"},
+            "config": workload_config(args, nw),
             "el_per_s": nw * args.steps * world / m_el,
             "fp64": {"walker_steps_per_s": units * world / f_met,
                      "el_per_s": nw * args.steps * world / f_el,
@@ -401,16 +410,16 @@ def run_reference(args):
     if rank != 0:
         return
     t0 = time.perf_counter()
-    cpu = cpu_baseline(args.cpu_seconds / max(args.steps, 1), steps=args.steps + args.warmup)
+    cpu = cpu_baseline(args.cpu_seconds / max(args.steps, 1), steps=args.steps,
+                       warmup=args.warmup)
     line = {
         "impl": "reference",
-        "metric": "walker-steps/s (Metropolis all-electron; E_L/s alongside)",
+        "metric": METRIC,
         "value": cpu["value"], "unit": "walker-steps/s", "n_gpus": int(os.environ.get(
             "WORLD_SIZE", "1")), "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": None, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "h2o_ccpvdz_single_double44_16384w", "configs": CONFIGS,
-                   "step_size": STEP_SIZE},
+        "ms_per_step": cpu["ms_per_round"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded walker positions)",
+        "config": workload_config(args, args.nwalkers),
         "cpu_baseline": cpu,
         "e2e": {"value": cpu["value"], "unit": "walker-steps/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},

@@ -48,10 +48,13 @@ enum qmc_status {
 
 /* Arithmetic of the fused kernels. QMC_PREC_FP64: the plain method, FP64
    throughout. QMC_PREC_MIXED: AO values and derivatives, the AO->MO
-   contraction, the Jastrow factor and the Slater LU in FP32; electron-nucleus
-   and electron-electron differences formed in FP64 before rounding; spin
-   determinants, psi, local-energy sums and one iterative-refinement step of
-   the solves that feed the kinetic energy in FP64. The staged module kernels
+   contraction, the Jastrow factor and the Slater LU in FP32; positions and
+   atom coordinates held as unevaluated FP32 pairs (hi + lo), so that
+   electron-nucleus and electron-electron differences keep FP64-level
+   accuracy in FP32 arithmetic; spin determinant products, psi, local-energy
+   sums and one iterative-refinement step of the solves that feed the kinetic
+   energy in FP64; CI sums as FP32 ratios to the ground-state determinant
+   scaled by its FP64 value. The staged module kernels
    (qmc_ao_eval, qmc_mo_eval, qmc_jastrow_ee, qmc_slater) are FP64 always. */
 #define QMC_PREC_FP64 0
 #define QMC_PREC_MIXED 1
