@@ -23,7 +23,7 @@ BUILD = os.path.join(ROOT, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
-           "qmc_probe.cu", "qmc_adjoint.cu"]
+           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 

@@ -282,6 +282,30 @@ __device__ __forceinline__ void group_d(const Tables<R>& t, int g, R dx, R dy, R
                               vs(5)));
 }
 
+// The AOs of group g at electron-atom difference (dx, dy, dz), r2 = |d|^2.
+template <typename R, bool DERIV, typename F>
+__device__ __forceinline__ void ao_group(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
+  const int nc = t.group_ao[g + 1] - t.group_ao[g];
+  switch (t.group_kind[g]) {
+    case GK_S:
+      if (nc == 1) group_s<R, DERIV, 1>(t, g, dx, dy, dz, r2, f);
+      else if (nc == 2) group_s<R, DERIV, 2>(t, g, dx, dy, dz, r2, f);
+      else group_generic<R, DERIV, QMC_MAX_COMP>(t, g, dx, dy, dz, r2, f);
+      break;
+    case GK_P: group_p<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
+    case GK_D: group_d<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
+    default:
+      switch (nc) {
+        case 1: group_generic<R, DERIV, 1>(t, g, dx, dy, dz, r2, f); break;
+        case 2: group_generic<R, DERIV, 2>(t, g, dx, dy, dz, r2, f); break;
+        case 3: group_generic<R, DERIV, 3>(t, g, dx, dy, dz, r2, f); break;
+        case 4: group_generic<R, DERIV, 4>(t, g, dx, dy, dz, r2, f); break;
+        case 5: group_generic<R, DERIV, 5>(t, g, dx, dy, dz, r2, f); break;
+        default: group_generic<R, DERIV, 6>(t, g, dx, dy, dz, r2, f); break;
+      }
+  }
+}
+
 // All AOs of one electron (split coordinates ex, ey, ez); the electron-atom
 // difference is formed once per atom (groups are stored atom by atom).
 template <typename R, bool DERIV, typename F>
@@ -298,25 +322,7 @@ __device__ __forceinline__ void for_each_ao_ep(const Tables<R>& t, XP<R> ex, XP<
       r2 = dx * dx + dy * dy + dz * dz;
       last = A;
     }
-    const int nc = t.group_ao[g + 1] - t.group_ao[g];
-    switch (t.group_kind[g]) {
-      case GK_S:
-        if (nc == 1) group_s<R, DERIV, 1>(t, g, dx, dy, dz, r2, f);
-        else if (nc == 2) group_s<R, DERIV, 2>(t, g, dx, dy, dz, r2, f);
-        else group_generic<R, DERIV, QMC_MAX_COMP>(t, g, dx, dy, dz, r2, f);
-        break;
-      case GK_P: group_p<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
-      case GK_D: group_d<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
-      default:
-        switch (nc) {
-          case 1: group_generic<R, DERIV, 1>(t, g, dx, dy, dz, r2, f); break;
-          case 2: group_generic<R, DERIV, 2>(t, g, dx, dy, dz, r2, f); break;
-          case 3: group_generic<R, DERIV, 3>(t, g, dx, dy, dz, r2, f); break;
-          case 4: group_generic<R, DERIV, 4>(t, g, dx, dy, dz, r2, f); break;
-          case 5: group_generic<R, DERIV, 5>(t, g, dx, dy, dz, r2, f); break;
-          default: group_generic<R, DERIV, 6>(t, g, dx, dy, dz, r2, f); break;
-        }
-    }
+    ao_group<R, DERIV>(t, g, dx, dy, dz, r2, f);
   }
 }
 

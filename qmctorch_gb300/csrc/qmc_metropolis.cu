@@ -4,61 +4,9 @@
 
 #include "qmc_ep.cuh"
 #include "qmc_host.cuh"
+#include "qmc_rng.cuh"
 
 namespace qmc {
-
-// ---------------------------------------------------------------------------
-// Metropolis
-// ---------------------------------------------------------------------------
-// Philox4x32-10 (Salmon, Moraes, Dror, Shaw, "Parallel random numbers: as easy
-// as 1, 2, 3", SC'11): 10 rounds of the 4x32 bijection with the published
-// multipliers and Weyl key increments.
-struct U4 {
-  uint32_t x, y, z, w;
-};
-__device__ __forceinline__ U4 philox(U4 c, uint32_t k0, uint32_t k1) {
-#pragma unroll
-  for (int r = 0; r < 10; ++r) {
-    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
-    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
-    c = U4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
-    k0 += 0x9E3779B9u;
-    k1 += 0xBB67AE85u;
-  }
-  return c;
-}
-
-struct Rng {
-  uint32_t k0, k1, walker;
-  uint64_t step;
-  uint32_t call;
-  __device__ __forceinline__ U4 next() {
-    return philox(U4{call++, walker, (uint32_t)step, (uint32_t)(step >> 32)}, k0, k1);
-  }
-  // two standard normals from two 32-bit words (Box-Muller, FP32 transcendentals)
-  __device__ __forceinline__ void normal2(uint32_t a, uint32_t b, double& z0, double& z1) {
-    const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;  // (0, 1]
-    const float u2 = (float)b * 2.3283064365386963e-10f;           // [0, 1)
-    const float rad = sqrtf(-2.0f * logf(u1));
-    float s, c;
-    sincospif(2.0f * u2, &s, &c);
-    z0 = (double)(rad * c);
-    z1 = (double)(rad * s);
-  }
-  __device__ __forceinline__ void normal2f(uint32_t a, uint32_t b, float& z0, float& z1) {
-    const float u1 = ((float)a + 1.0f) * 2.3283064365386963e-10f;
-    const float u2 = (float)b * 2.3283064365386963e-10f;
-    const float rad = sqrtf(-2.0f * logf(u1));
-    float s, c;
-    sincospif(2.0f * u2, &s, &c);
-    z0 = rad * c;
-    z1 = rad * s;
-  }
-  // uniform in [0, 1) with 53 random bits
-  __device__ __forceinline__ double uniform53(uint32_t hi, uint32_t lo) {
-    return ((double)(hi >> 5) * 67108864.0 + (double)(lo >> 6)) * 1.1102230246251565e-16;
-  }
-};
 
 // One block advances `nwb` walker chains through all steps. Per move: every
 // electron thread writes its proposed coordinates (Philox normals or the
@@ -116,9 +64,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
             if (a.proposals) {
               iel = a.electron_index[(int64_t)istep * nw + w0 + tid];
             } else {
-              rng.call = call0 + ne + 1;
-              const U4 r = rng.next();
-              iel = (int)(((uint64_t)r.x * (uint64_t)ne) >> 32);
+              iel = electron_draw(rng, call0 + ne + 1, ne);
             }
           }
           IEL[tid] = iel;
@@ -131,31 +77,13 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
                                     (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]));
         XP<R>* pn = PN + wl * nc + 3 * e;
         const XP<R>* pc = P + wl * nc + 3 * e;
-        if (moves && a.proposals) {
-          const double* pr = a.move_type == QMC_MOVE_ALL_ELEC
-                                 ? a.proposals + ((int64_t)istep * nw + w) * nc + 3 * e
-                                 : a.proposals + (((int64_t)istep * nmove + im) * nw + w) * 3;
-          for (int q = 0; q < 3; ++q) {
-            const R zh = (R)pr[q];
-            pn[q] = xp_add<R>(pc[q], zh, (R)(pr[q] - (double)zh));
-          }
-        } else if (moves) {
-          rng.call = call0 + e;
-          const U4 r = rng.next();
-          R z[3];
-          if (a.proba == QMC_PROBA_NORMAL) {
-            float f0, f1, f2, f3;
-            rng.normal2f(r.x, r.y, f0, f1);
-            rng.normal2f(r.z, r.w, f2, f3);
-            z[0] = (R)f0 * (R)sd;
-            z[1] = (R)f1 * (R)sd;
-            z[2] = (R)f2 * (R)sd;
-          } else {
-            const uint32_t rr[3] = {r.x, r.y, r.z};
-            for (int q = 0; q < 3; ++q)
-              z[q] = (R)a.step_size * ((R)2 * ((R)rr[q] * (R)2.3283064365386963e-10) - (R)1);
-          }
-          for (int q = 0; q < 3; ++q) pn[q] = xp_add<R>(pc[q], z[q]);
+        if (moves) {
+          const double* rp =
+              !a.proposals ? nullptr
+              : a.move_type == QMC_MOVE_ALL_ELEC
+                  ? a.proposals + ((int64_t)istep * nw + w) * nc + 3 * e
+                  : a.proposals + (((int64_t)istep * nmove + im) * nw + w) * 3;
+          propose_electron<R>(rng, call0 + e, a.proba, a.step_size, sd, rp, pc, pn);
         } else {
           for (int q = 0; q < 3; ++q) pn[q] = pc[q];
         }
@@ -170,9 +98,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
                   ? a.uniforms[(int64_t)istep * nw + w0 + tid]
                   : a.uniforms[((int64_t)istep * nmove + im) * nw + w0 + tid];
         } else {
-          rng.call = call0 + ne;
-          const U4 r = rng.next();
-          u = rng.uniform53(r.x, r.y);
+          u = accept_uniform(rng, call0 + ne);
         }
         double fxn = PSI[tid] * PSI[tid];
         if (fxn == 0.0) fxn = eps;
@@ -229,6 +155,10 @@ static int launch_metropolis(const qmc_wf_desc* d, const qmc_metropolis_args* a,
 
 using namespace qmc;
 
+// qmc_sweep.cu: Sherman-Morrison single-electron moves
+int qmc_sweep_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void* stream);
+bool qmc_sweep_eligible(const qmc_wf_desc* d, const qmc_metropolis_args* a);
+
 extern "C" {
 
 int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void* scratch,
@@ -243,6 +173,7 @@ int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void*
   if (a->proposals && !a->uniforms) return QMC_ERR_ARG;
   if (a->proposals && a->move_type == QMC_MOVE_ONE_ELEC && !a->electron_index) return QMC_ERR_ARG;
   if (scratch_bytes < qmc_metropolis_scratch_bytes(d, a->nwalkers)) return QMC_ERR_SCRATCH;
+  if (qmc_sweep_eligible(d, a)) return qmc_sweep_run(d, a, stream);
   cudaStream_t s = (cudaStream_t)stream;
   unsigned char* scr = (unsigned char*)scratch;
   if (d->precision == QMC_PREC_MIXED) {

@@ -3,7 +3,7 @@ QMCTorch package itself (FP64, CPU) on seeded inputs.
 
 Usage (in a container where the reference source tree is available):
 
-    python tests/golden/make_golden.py /path/to/QMCTorch
+    python tests/golden/make_golden.py /path/to/QMCTorch [case ...]
 
 Writes ``tests/golden/<case>.npz``. Each file holds the molecule / basis
 namespace (``mol_*`` / ``basis_*`` keys, the layout of
@@ -38,11 +38,11 @@ CASES = {
     "h2o_single": ("O 0 0 0.1173; H 0 0.7572 -0.4692; H 0 -0.7572 -0.4692", "angs", "cc-pvdz",
                    "single(2,2)", True, 6, True, ()),
     "h4": ("H 0 0 0; H 0 0 1.0; H 0 0 2.0; H 0 0 3.0", "angs", "sto-3g", "ground_state",
-           False, 8, False, ("metropolis",)),
+           False, 8, False, ("metropolis", "iter", "oneelec")),
     "c6h6": ("C 1.39 0 0; C 0.695 1.20377 0; C -0.695 1.20377 0; C -1.39 0 0; "
              "C -0.695 -1.20377 0; C 0.695 -1.20377 0; H 2.48 0 0; H 1.24 2.14774 0; "
              "H -1.24 2.14774 0; H -2.48 0 0; H -1.24 -2.14774 0; H 1.24 -2.14774 0",
-             "angs", "cc-pvdz", "ground_state", True, 3, False, ()),
+             "angs", "cc-pvdz", "ground_state", True, 3, False, ("iter", "oneelec")),
 }
 
 
@@ -58,7 +58,7 @@ def seeded_positions(mol, nw, seed):
     return pos.reshape(nw, -1)
 
 
-def main(reference_root):
+def main(reference_root, only=()):
     ref_stubs.install(reference_root)
     import torch
     from qmctorch.utils import set_torch_double_precision
@@ -70,6 +70,8 @@ def main(reference_root):
 
     set_torch_double_precision()
     for name, (atoms, unit, basis, configs, all_mo, nw, random_ci, extras) in CASES.items():
+        if only and name not in only:
+            continue
         torch.manual_seed(1234)
         mol = Molecule(atoms, unit=unit, basis=basis)
         tmp = os.path.join(HERE, "_tmp_mol.npz")
@@ -148,6 +150,34 @@ def main(reference_root):
             data.update(iter_pos0=pos0, iter_props=props, iter_unif=unif,
                         iter_out=out.detach().numpy())
 
+        if "oneelec" in extras:
+            rng = np.random.default_rng(23)
+            mnw, nstep, step = 6, 10, 0.3
+            sig = np.sqrt(step / (2 * np.sqrt(2 * np.log(2))))
+            props = rng.normal(size=(nstep, mnw, 3)) * sig
+            unif = rng.uniform(size=(nstep, mnw))
+            pos0 = seeded_positions(mol, mnw, seed=7)
+            sampler = Metropolis(nwalkers=mnw, nstep=nstep, step_size=step, ntherm=2,
+                                 ndecor=3, nelec=mol.nelec, init=mol.domain("atomic"),
+                                 move={"type": "one-elec", "proba": "normal"})
+            it_p = iter(torch.as_tensor(props))
+            it_u = iter(torch.as_tensor(unif))
+            sampler._move = types.MethodType(lambda self, n: next(it_p), sampler)
+            orig = qmet.torch.rand_like
+            qmet.torch.rand_like = lambda t: next(it_u).reshape(t.shape).type(t.dtype)
+            # the electron indices are the only draws left on torch's generator
+            torch.manual_seed(99)
+            try:
+                out = sampler(wf.pdf, pos=torch.tensor(pos0), with_tqdm=False)
+            finally:
+                qmet.torch.rand_like = orig
+            torch.manual_seed(99)
+            index = np.stack([torch.LongTensor(mnw).random_(0, mol.nelec).numpy()
+                              for _ in range(nstep)])
+            data.update(one_pos0=pos0, one_props=props, one_unif=unif, one_index=index,
+                        one_step=np.asarray(step), one_ntherm=np.asarray(2),
+                        one_ndecor=np.asarray(3), one_out=out.detach().numpy())
+
         if "solver" in extras:
             sampler = Metropolis(nwalkers=nw, nstep=2, step_size=0.2, nelec=mol.nelec,
                                  init=mol.domain("atomic"))
@@ -174,4 +204,4 @@ def main(reference_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", tuple(sys.argv[2:]))

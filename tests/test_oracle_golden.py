@@ -57,12 +57,28 @@ def test_oracle_metropolis_replay(name):
     close(out, d["met_out"])
 
 
-def test_oracle_metropolis_iter_replay():
-    mol, d = load("h2o_sd")
+@pytest.mark.parametrize("name", [c for c in CASES if "iter_out" in load(c)[1]])
+def test_oracle_metropolis_iter_replay(name):
+    mol, d = load(name)
     wf = _oracle(mol, d)
     out, _, _ = orc.metropolis_replay(wf.pdf, d["iter_pos0"], d["iter_props"], d["iter_unif"],
                                       move_type="all-elec-iter")
     close(out, d["iter_out"])
+
+
+@pytest.mark.parametrize("name", [c for c in CASES if "one_out" in load(c)[1]])
+def test_oracle_metropolis_one_elec_replay(name):
+    """one-elec moves: the electron index each walker moves per step was drawn
+    by the reference (torch.LongTensor.random_, metropolis.py:247) and is
+    replayed with its proposals and uniforms."""
+    mol, d = load(name)
+    wf = _oracle(mol, d)
+    nstep, nw = d["one_unif"].shape
+    out, _, _ = orc.metropolis_replay(wf.pdf, d["one_pos0"], d["one_props"][:, None],
+                                      d["one_unif"][:, None], ntherm=int(d["one_ntherm"]),
+                                      ndecor=int(d["one_ndecor"]), move_type="one-elec",
+                                      electron_index=d["one_index"][:, None])
+    close(out, d["one_out"])
 
 
 def test_configs_match_reference_counts():
