@@ -138,7 +138,11 @@ __host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
 // AO groups
 // ---------------------------------------------------------------------------
 // Radial sums G_n = sum_p w_cp alpha_p^n exp(-alpha_p r^2) of NC components.
-template <typename R, bool DERIV, int NC>
+// CUT: skip primitives with alpha r^2 > kRadialCut (exp < 1e-20), for the
+// single-electron ratio kernel only; every other kernel evaluates all terms.
+constexpr float kRadialCut = 46.0f;
+
+template <typename R, bool DERIV, int NC, bool CUT = false>
 __device__ __forceinline__ void group_radial(const Tables<R>& t, int g, R r2, R (&G0)[NC],
                                              R (&G1)[NC], R (&G2)[NC]) {
   const int p0 = t.group_prim[g], np = t.group_prim[g + 1] - p0;
@@ -148,6 +152,7 @@ __device__ __forceinline__ void group_radial(const Tables<R>& t, int g, R r2, R 
   if (!t.group_split[g]) {
     for (int p = 0; p < np; ++p) {
       const R al = t.alpha[p0 + p];
+      if (CUT && al * r2 > (R)kRadialCut) continue;
       const R e0 = rexp(-al * r2);
       const R e1 = al * e0, e2 = al * e1;
 #pragma unroll
@@ -167,6 +172,7 @@ __device__ __forceinline__ void group_radial(const Tables<R>& t, int g, R r2, R 
       for (int c = 0; c < NC; ++c) {
         const int wi = wb + c * np + p;
         const R al = t.walpha[wi];
+        if (CUT && al * r2 > (R)kRadialCut) continue;
         const R e0 = rexp(-al * r2);
         const R w = t.wd[wi];
         G0[c] = fma(w, e0, G0[c]);
@@ -211,11 +217,11 @@ __device__ __forceinline__ R pk2(R x, int k) {
   return k < 2 ? (R)0 : (k == 2 ? (R)2 : (R)(k * (k - 1)) * ipow(x, k - 2));
 }
 
-template <typename R, bool DERIV, int NC, typename F>
+template <typename R, bool DERIV, int NC, typename F, bool CUT = false>
 __device__ __forceinline__ void group_generic(const Tables<R>& t, int g, R dx, R dy, R dz, R r2,
                                               F& f) {
   R G0[NC], G1[NC], G2[NC];
-  group_radial<R, DERIV, NC>(t, g, r2, G0, G1, G2);
+  group_radial<R, DERIV, NC, CUT>(t, g, r2, G0, G1, G2);
   const int a0 = t.group_ao[g];
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
@@ -235,10 +241,10 @@ __device__ __forceinline__ void group_generic(const Tables<R>& t, int g, R dx, R
   }
 }
 
-template <typename R, bool DERIV, int NC, typename F>
+template <typename R, bool DERIV, int NC, typename F, bool CUT = false>
 __device__ __forceinline__ void group_s(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
   R G0[NC], G1[NC], G2[NC];
-  group_radial<R, DERIV, NC>(t, g, r2, G0, G1, G2);
+  group_radial<R, DERIV, NC, CUT>(t, g, r2, G0, G1, G2);
   const int a0 = t.group_ao[g];
 #pragma unroll
   for (int c = 0; c < NC; ++c) {
@@ -248,10 +254,10 @@ __device__ __forceinline__ void group_s(const Tables<R>& t, int g, R dx, R dy, R
   }
 }
 
-template <typename R, bool DERIV, typename F>
+template <typename R, bool DERIV, typename F, bool CUT = false>
 __device__ __forceinline__ void group_p(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
   R G0[3], G1[3], G2[3];
-  group_radial<R, DERIV, 3>(t, g, r2, G0, G1, G2);
+  group_radial<R, DERIV, 3, CUT>(t, g, r2, G0, G1, G2);
   const int a0 = t.group_ao[g];
   const R o = (R)0, i = (R)1;
   auto vs = [&](int c) { return t.vscale ? t.vscale[a0 + c] : (R)1; };
@@ -261,10 +267,10 @@ __device__ __forceinline__ void group_p(const Tables<R>& t, int g, R dx, R dy, R
 }
 
 // cartesian d shell, components xx, xy, xz, yy, yz, zz (pyscf.py:120-122)
-template <typename R, bool DERIV, typename F>
+template <typename R, bool DERIV, typename F, bool CUT = false>
 __device__ __forceinline__ void group_d(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
   R G0[6], G1[6], G2[6];
-  group_radial<R, DERIV, 6>(t, g, r2, G0, G1, G2);
+  group_radial<R, DERIV, 6, CUT>(t, g, r2, G0, G1, G2);
   const int a0 = t.group_ao[g];
   const R o = (R)0, two = (R)2;
   auto vs = [&](int c) { return t.vscale ? t.vscale[a0 + c] : (R)1; };
@@ -283,25 +289,25 @@ __device__ __forceinline__ void group_d(const Tables<R>& t, int g, R dx, R dy, R
 }
 
 // The AOs of group g at electron-atom difference (dx, dy, dz), r2 = |d|^2.
-template <typename R, bool DERIV, typename F>
+template <typename R, bool DERIV, typename F, bool CUT = false>
 __device__ __forceinline__ void ao_group(const Tables<R>& t, int g, R dx, R dy, R dz, R r2, F& f) {
   const int nc = t.group_ao[g + 1] - t.group_ao[g];
   switch (t.group_kind[g]) {
     case GK_S:
-      if (nc == 1) group_s<R, DERIV, 1>(t, g, dx, dy, dz, r2, f);
-      else if (nc == 2) group_s<R, DERIV, 2>(t, g, dx, dy, dz, r2, f);
-      else group_generic<R, DERIV, QMC_MAX_COMP>(t, g, dx, dy, dz, r2, f);
+      if (nc == 1) group_s<R, DERIV, 1, F, CUT>(t, g, dx, dy, dz, r2, f);
+      else if (nc == 2) group_s<R, DERIV, 2, F, CUT>(t, g, dx, dy, dz, r2, f);
+      else group_generic<R, DERIV, QMC_MAX_COMP, F, CUT>(t, g, dx, dy, dz, r2, f);
       break;
-    case GK_P: group_p<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
-    case GK_D: group_d<R, DERIV>(t, g, dx, dy, dz, r2, f); break;
+    case GK_P: group_p<R, DERIV, F, CUT>(t, g, dx, dy, dz, r2, f); break;
+    case GK_D: group_d<R, DERIV, F, CUT>(t, g, dx, dy, dz, r2, f); break;
     default:
       switch (nc) {
-        case 1: group_generic<R, DERIV, 1>(t, g, dx, dy, dz, r2, f); break;
-        case 2: group_generic<R, DERIV, 2>(t, g, dx, dy, dz, r2, f); break;
-        case 3: group_generic<R, DERIV, 3>(t, g, dx, dy, dz, r2, f); break;
-        case 4: group_generic<R, DERIV, 4>(t, g, dx, dy, dz, r2, f); break;
-        case 5: group_generic<R, DERIV, 5>(t, g, dx, dy, dz, r2, f); break;
-        default: group_generic<R, DERIV, 6>(t, g, dx, dy, dz, r2, f); break;
+        case 1: group_generic<R, DERIV, 1, F, CUT>(t, g, dx, dy, dz, r2, f); break;
+        case 2: group_generic<R, DERIV, 2, F, CUT>(t, g, dx, dy, dz, r2, f); break;
+        case 3: group_generic<R, DERIV, 3, F, CUT>(t, g, dx, dy, dz, r2, f); break;
+        case 4: group_generic<R, DERIV, 4, F, CUT>(t, g, dx, dy, dz, r2, f); break;
+        case 5: group_generic<R, DERIV, 5, F, CUT>(t, g, dx, dy, dz, r2, f); break;
+        default: group_generic<R, DERIV, 6, F, CUT>(t, g, dx, dy, dz, r2, f); break;
       }
   }
 }

@@ -56,23 +56,13 @@ struct Rng {
   }
 };
 
-// Proposed coordinates of one electron: pc + displacement, the displacement
-// either replayed (rp: three FP64 values) or drawn with counter `call`
-// (normal: two Box-Muller pairs scaled by sd; uniform: step * (2u - 1)).
+// Generated displacement of one electron, counter `call` (normal: two
+// Box-Muller pairs scaled by sd; uniform: step * (2u - 1)).
 template <typename R>
-__device__ __forceinline__ void propose_electron(Rng& rng, uint32_t call, int proba, double step,
-                                                 double sd, const double* rp, const XP<R>* pc,
-                                                 XP<R>* pn) {
-  if (rp) {
-    for (int q = 0; q < 3; ++q) {
-      const R zh = (R)rp[q];
-      pn[q] = xp_add<R>(pc[q], zh, (R)(rp[q] - (double)zh));
-    }
-    return;
-  }
+__device__ __forceinline__ void draw_displacement(Rng& rng, uint32_t call, int proba, double step,
+                                                  double sd, R (&z)[3]) {
   rng.call = call;
   const U4 r = rng.next();
-  R z[3];
   if (proba == QMC_PROBA_NORMAL) {
     float f0, f1, f2, f3;
     rng.normal2f(r.x, r.y, f0, f1);
@@ -85,6 +75,30 @@ __device__ __forceinline__ void propose_electron(Rng& rng, uint32_t call, int pr
     for (int q = 0; q < 3; ++q)
       z[q] = (R)step * ((R)2 * ((R)rr[q] * (R)2.3283064365386963e-10) - (R)1);
   }
+}
+
+// Replayed displacement (three FP64 values): pn = pc + rp, keeping in the
+// low part of a split coordinate what FP32 cannot hold.
+template <typename R>
+__device__ __forceinline__ void replay_displacement(const double* rp, const XP<R>* pc, XP<R>* pn) {
+  for (int q = 0; q < 3; ++q) {
+    const R zh = (R)rp[q];
+    pn[q] = xp_add<R>(pc[q], zh, (R)(rp[q] - (double)zh));
+  }
+}
+
+// Proposed coordinates of one electron: pc + displacement, the displacement
+// either replayed (rp: three FP64 values) or drawn with counter `call`.
+template <typename R>
+__device__ __forceinline__ void propose_electron(Rng& rng, uint32_t call, int proba, double step,
+                                                 double sd, const double* rp, const XP<R>* pc,
+                                                 XP<R>* pn) {
+  if (rp) {
+    replay_displacement<R>(rp, pc, pn);
+    return;
+  }
+  R z[3];
+  draw_displacement<R>(rng, call, proba, step, sd, z);
   for (int q = 0; q < 3; ++q) pn[q] = xp_add<R>(pc[q], z[q]);
 }
 

@@ -32,11 +32,19 @@ struct SweepShape {
   int n[2];      // electrons per spin
   int ld[2];     // row stride of A_s^-1 (odd: conflict-free column access)
   int nmax, ldm; // Gauss-Jordan work matrix
-  int64_t o_tab, o_warp, warp_bytes, smem;
-  int64_t o_p, o_v[2], o_m, o_ao, o_phi, o_y, o_col;
+  int64_t o_tab, o_gpatom, o_meta, o_aoord, o_wt, o_warp, warp_bytes, smem;
+  int64_t o_p, o_v[2], o_m, o_ao, o_phi, o_y, o_col, o_e, o_d;
 };
 
 inline int64_t align16(int64_t n) { return (n + 15) & ~int64_t(15); }
+
+// Row stride (entries) of the transposed MO coefficients WT: 16 bytes past a
+// multiple of 128, so that 16-byte loads of consecutive rows hit distinct banks.
+template <typename R>
+__host__ __device__ inline int wt_ld(int nao) {
+  const int bytes = ((pad4(nao) * (int)sizeof(R) + 127) / 128) * 128 + 16;
+  return bytes / (int)sizeof(R);
+}
 
 template <typename R>
 inline SweepShape sweep_shape(const qmc_wf_desc& d, int nww, int jc) {
@@ -52,7 +60,11 @@ inline SweepShape sweep_shape(const qmc_wf_desc& d, int nww, int jc) {
   s.ncol = round_up(s.nmax > 0 ? s.nmax : 1, jc);  // whole JC-column chunks
   const int64_t rs = sizeof(R);
   s.o_tab = 0;
-  s.o_warp = align16(tables_smem_bytes<R>(d, s.ncol));
+  s.o_gpatom = align16(tables_smem_bytes<R>(d, s.ncol));
+  s.o_meta = s.o_gpatom + align16((int64_t)d.ngprim * 4);
+  s.o_aoord = s.o_meta + align16((int64_t)d.nao * 16);
+  s.o_wt = s.o_aoord + align16((int64_t)round_up(d.nao, 32) * 4);
+  s.o_warp = s.o_wt + align16((int64_t)s.nmax * wt_ld<R>(d.nao) * rs);
   int64_t q = 0;
   s.o_p = q;
   q += align16(3 * (int64_t)d.nelec * (int64_t)sizeof(XP<R>));
@@ -63,13 +75,17 @@ inline SweepShape sweep_shape(const qmc_wf_desc& d, int nww, int jc) {
   s.o_m = q;
   q += align16((int64_t)s.nmax * s.ldm * rs);
   s.o_ao = q;
-  q += align16((int64_t)d.nao * rs);
+  q += align16((int64_t)pad4(d.nao) * rs);
   s.o_phi = q;
   q += align16((int64_t)s.nmax * rs);
   s.o_y = q;
   q += align16((int64_t)s.nmax * rs);
   s.o_col = q;
   q += align16((int64_t)s.nmax * rs);
+  s.o_e = q;
+  q += align16((int64_t)d.ngprim * rs);
+  s.o_d = q;
+  q += align16((int64_t)d.natom * 4 * rs);
   s.warp_bytes = q;
   s.smem = s.o_warp + (int64_t)nww * q;
   return s;
@@ -77,36 +93,135 @@ inline SweepShape sweep_shape(const qmc_wf_desc& d, int nww, int jc) {
 
 constexpr unsigned kFull = 0xffffffffu;
 
-// AO values of one electron at (ex, ey, ez) into AO[0..nao): the warp's
-// lanes take the groups round-robin.
+// Per-block tables of the single-electron AO and MO rows:
+// * gp_atom4[i] = 4 x atom of group primitive i (offset into D);
+// * meta[a] = {4 x atom, p0 | np << 16, weight offset, kx | ky << 8 | kz << 16
+//   | split << 24} of AO a, read with one 16-byte load;
+// * ao_ord: the order in which the lanes take the AOs (ranked by primitive
+//   count, dealt in a snake order so that the lanes holding the longest sums
+//   in one round get the shortest in the next), -1 = none;
+// * WT[j][a] = W[a][j] for j < nmax, rows of ldt entries (16 bytes past a
+//   multiple of 128: conflict-free 16-byte loads), zero past nao.
+struct AORowTabs {
+  const int* gp_atom4;  // [ngprim]
+  const int4* meta;     // [nao]
+  const int* ao_ord;    // [round_up(nao, 32)]
+};
+
 template <typename R>
-__device__ inline void warp_ao_row(const Tables<R>& t, XP<R> ex, XP<R> ey, XP<R> ez, R* AO,
-                                   int lane) {
-  auto put = [&](int a, const AOVal<R>& o) { AO[a] = o.v; };
-  for (int g = lane; g < t.ngroup; g += 32) {
-    const int A = t.group_atom[g];
+__device__ inline AORowTabs build_ao_row_tabs(const Tables<R>& t, int nmax, int* gp_atom4,
+                                              int4* meta, int* ao_ord, R* WT) {
+  const int tid = threadIdx.x, nt = blockDim.x, nslot = round_up(t.nao, 32);
+  for (int g = tid; g < t.ngroup; g += nt) {
+    const int p0 = t.group_prim[g], np = t.group_prim[g + 1] - p0, A4 = 4 * t.group_atom[g];
+    for (int p = p0; p < p0 + np; ++p) gp_atom4[p] = A4;
+    for (int a = t.group_ao[g]; a < t.group_ao[g + 1]; ++a)
+      meta[a] = make_int4(A4, p0 | (np << 16), t.ao_wofs[a],
+                          t.ao_k[3 * a] | (t.ao_k[3 * a + 1] << 8) | (t.ao_k[3 * a + 2] << 16) |
+                              (t.group_split[g] << 24));
+  }
+  for (int i = tid; i < nslot; i += nt) ao_ord[i] = -1;
+  const int ldt = wt_ld<R>(t.nao);
+  for (int i = tid; i < nmax * ldt; i += nt) {
+    const int j = i / ldt, a = i - j * ldt;
+    WT[i] = a < t.nao ? t.W[a * t.ncol + j] : (R)0;
+  }
+  __syncthreads();
+  auto np = [&](int a) { return meta[a].y >> 16; };
+  for (int a = tid; a < t.nao; a += nt) {
+    const int c = np(a);
+    int r = 0;
+    for (int b = 0; b < t.nao; ++b) {
+      const int cb = np(b);
+      r += (cb > c) || (cb == c && b < a);
+    }
+    const int round = r >> 5, pos = r & 31;
+    ao_ord[32 * round + ((round & 1) ? 31 - pos : pos)] = a;
+  }
+  __syncthreads();
+  return AORowTabs{gp_atom4, meta, ao_ord};
+}
+
+// 16-byte aligned groups of four values (AO rows and WT rows are padded).
+__device__ __forceinline__ void ld4(const float* p, float (&v)[4]) {
+  const float4 q = *reinterpret_cast<const float4*>(p);
+  v[0] = q.x;
+  v[1] = q.y;
+  v[2] = q.z;
+  v[3] = q.w;
+}
+__device__ __forceinline__ void ld4(const double* p, double (&v)[4]) {
+  const double2 q0 = *reinterpret_cast<const double2*>(p);
+  const double2 q1 = *reinterpret_cast<const double2*>(p + 2);
+  v[0] = q0.x;
+  v[1] = q0.y;
+  v[2] = q1.x;
+  v[3] = q1.y;
+}
+
+// AO values of one electron at (ex, ey, ez) into AO[0..nao) in three
+// warp-uniform phases: electron-atom differences (D[4A..4A+3] = dx, dy, dz,
+// r^2), one exp per group primitive (E), then per AO its polynomial times
+// sum_p w_p E_p. The plain method skips exps with alpha r^2 > kRadialCut.
+template <typename R>
+__device__ inline void warp_ao_row(const Tables<R>& t, const AORowTabs& x, XP<R> ex, XP<R> ey,
+                                   XP<R> ez, R* E, R* D, R* AO, int lane) {
+  for (int A = lane; A < t.natom; A += 32) {
     const R dx = dif(ex, t.atom_p[3 * A]), dy = dif(ey, t.atom_p[3 * A + 1]),
             dz = dif(ez, t.atom_p[3 * A + 2]);
-    ao_group<R, false>(t, g, dx, dy, dz, dx * dx + dy * dy + dz * dz, put);
+    D[4 * A] = dx;
+    D[4 * A + 1] = dy;
+    D[4 * A + 2] = dz;
+    D[4 * A + 3] = dx * dx + dy * dy + dz * dz;
+  }
+  __syncwarp();
+  const int ngp = t.group_prim[t.ngroup];
+  for (int i = lane; i < ngp; i += 32) {
+    const R ar = t.alpha[i] * D[x.gp_atom4[i] + 3];
+    E[i] = (!kMixed<R> && ar > (R)kRadialCut) ? (R)0 : rexp(-ar);
+  }
+  __syncwarp();
+  const int nslot = round_up(t.nao, 32);
+  for (int k = lane; k < nslot; k += 32) {
+    const int a = x.ao_ord[k];
+    if (a < 0) continue;
+    const int4 m = x.meta[a];
+    R dd[4];
+    ld4(D + m.x, dd);
+    const int p0 = m.y & 0xffff, np = m.y >> 16;
+    const R* wp = t.wd + m.z;
+    R G = (R)0;
+    if (!(m.w >> 24)) {
+      const R* ep = E + p0;
+      for (int p = 0; p < np; ++p) G = fma(wp[p], ep[p], G);
+    } else {  // components with their own exponents
+      const R* ap = t.walpha + m.z;
+      for (int p = 0; p < np; ++p) G = fma(wp[p], rexp(-ap[p] * dd[3]), G);
+    }
+    const R P = pk0(dd[0], m.w & 0xff) * pk0(dd[1], (m.w >> 8) & 0xff) *
+                pk0(dd[2], (m.w >> 16) & 0xff);
+    AO[a] = (t.vscale ? t.vscale[a] : (R)1) * (P * G);
   }
   __syncwarp();
 }
 
-// out[j] = sum_a AO[a] W[a][j] for j < n (lane j; four partial sums).
+// out[j] = sum_a AO[a] WT[j][a] for j < n (lane j; 16-byte loads, four
+// partial sums; AO and WT rows zero-padded to a multiple of four).
 template <typename R>
-__device__ inline void warp_mo_row(const Tables<R>& t, const R* AO, int n, R* out, int lane) {
+__device__ inline void warp_mo_row_t(const R* WT, int ldt, int na4, const R* AO, int n, R* out,
+                                     int lane) {
   for (int j = lane; j < n; j += 32) {
+    const R* wr = WT + j * ldt;
     R s0 = (R)0, s1 = (R)0, s2 = (R)0, s3 = (R)0;
-    const R* wc = t.W + j;
-    const int nc = t.ncol, na = t.nao;
-    int a = 0;
-    for (; a + 3 < na; a += 4) {
-      s0 = fma(AO[a], wc[(int64_t)a * nc], s0);
-      s1 = fma(AO[a + 1], wc[(int64_t)(a + 1) * nc], s1);
-      s2 = fma(AO[a + 2], wc[(int64_t)(a + 2) * nc], s2);
-      s3 = fma(AO[a + 3], wc[(int64_t)(a + 3) * nc], s3);
+    for (int a = 0; a < na4; a += 4) {
+      R v[4], w[4];
+      ld4(AO + a, v);
+      ld4(wr + a, w);
+      s0 = fma(v[0], w[0], s0);
+      s1 = fma(v[1], w[1], s1);
+      s2 = fma(v[2], w[2], s2);
+      s3 = fma(v[3], w[3], s3);
     }
-    for (; a < na; ++a) s0 = fma(AO[a], wc[(int64_t)a * nc], s0);
     out[j] = (s0 + s1) + (s2 + s3);
   }
   __syncwarp();
@@ -205,6 +320,11 @@ __global__ void __launch_bounds__(256, kMixed<R> ? 3 : 2)
     sweep_kernel(const qmc_wf_desc d, const qmc_metropolis_args a, const SweepShape S) {
   extern __shared__ __align__(16) unsigned char smem[];
   const Tables<R> t = load_tables<R>(d, S.nmax, S.ncol, smem + S.o_tab);
+  R* const WT = reinterpret_cast<R*>(smem + S.o_wt);
+  const AORowTabs xt = build_ao_row_tabs<R>(t, S.nmax, reinterpret_cast<int*>(smem + S.o_gpatom),
+                                            reinterpret_cast<int4*>(smem + S.o_meta),
+                                            reinterpret_cast<int*>(smem + S.o_aoord), WT);
+  const int ldt = wt_ld<R>(d.nao), na4 = pad4(d.nao);
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int64_t nw = a.nwalkers;
   const int64_t w = (int64_t)blockIdx.x * S.nww + wib;
@@ -218,8 +338,11 @@ __global__ void __launch_bounds__(256, kMixed<R> ? 3 : 2)
   R* PHI = reinterpret_cast<R*>(base + S.o_phi);
   R* Y = reinterpret_cast<R*>(base + S.o_y);
   R* COL = reinterpret_cast<R*>(base + S.o_col);
+  R* E = reinterpret_cast<R*>(base + S.o_e);
+  R* D = reinterpret_cast<R*>(base + S.o_d);
   const int ne = d.nelec, nc = 3 * ne, nup = d.nup;
   for (int i = lane; i < nc; i += 32) P[i] = split_xp<R>(a.pos[w * nc + i]);
+  for (int i = d.nao + lane; i < pad4(d.nao); i += 32) AO[i] = (R)0;
   __syncwarp();
 
   auto rebuild = [&]() {
@@ -240,6 +363,13 @@ __global__ void __launch_bounds__(256, kMixed<R> ? 3 : 2)
   const int nmove = a.move_type == QMC_MOVE_ALL_ELEC_ITER ? ne : 1;
   int nacc = 0, since_rebuild = 0;
   int64_t isnap = 0, idecor = 0;
+  // Generated random numbers are drawn 32 moves at a time, lane k holding
+  // those of move base + k (moves of one step for all-elec-iter, steps for
+  // one-elec), and broadcast when the move comes.
+  R bz[3] = {(R)0, (R)0, (R)0};
+  double bu = 0.0;
+  int be = 0;
+  const bool iter = a.move_type == QMC_MOVE_ALL_ELEC_ITER;
   for (int istep = 0; istep < a.nstep; ++istep) {
     rng.step = a.step_offset + istep;
     for (int im = 0; im < nmove; ++im) {
@@ -248,24 +378,39 @@ __global__ void __launch_bounds__(256, kMixed<R> ? 3 : 2)
         since_rebuild = 0;
       }
       ++since_rebuild;
-      const uint32_t call0 = (uint32_t)im * (uint32_t)(ne + 2);
-      int e = im;
-      if (a.move_type == QMC_MOVE_ONE_ELEC)
-        e = a.proposals ? a.electron_index[(int64_t)istep * nw + w]
-                        : electron_draw(rng, call0 + ne + 1, ne);
+      const int slot = (iter ? im : istep) & 31;
+      if (!a.proposals && slot == 0) {
+        Rng r = rng;
+        int jm = im;
+        if (iter) {
+          jm = im + lane;
+        } else {
+          r.step = a.step_offset + istep + lane;
+        }
+        const uint32_t c0 = (uint32_t)jm * (uint32_t)(ne + 2);
+        be = iter ? jm : electron_draw(r, c0 + ne + 1, ne);
+        draw_displacement<R>(r, c0 + be, a.proba, a.step_size, sd, bz);
+        bu = accept_uniform(r, c0 + ne);
+      }
+      XP<R> pn[3];
+      double u;
+      int e;
+      if (a.proposals) {
+        e = iter ? im : a.electron_index[(int64_t)istep * nw + w];
+        const int64_t mv = ((int64_t)istep * nmove + im) * nw + w;
+        replay_displacement<R>(a.proposals + mv * 3, P + 3 * e, pn);
+        u = a.uniforms[mv];
+      } else {
+        e = __shfl_sync(kFull, be, slot);
+        u = __shfl_sync(kFull, bu, slot);
+        for (int q = 0; q < 3; ++q) pn[q] = xp_add<R>(P[3 * e + q], __shfl_sync(kFull, bz[q], slot));
+      }
       const int s = e < nup ? 0 : 1, l = e - s * nup;
       const int n = s ? S.n[1] : S.n[0], ld = s ? S.ld[1] : S.ld[0];
       R* const Vs = s ? V1 : V0;
-      // proposal: every lane derives the same coordinates
-      XP<R> pn[3];
-      const double* rp =
-          a.proposals ? a.proposals + (((int64_t)istep * nmove + im) * nw + w) * 3 : nullptr;
-      propose_electron<R>(rng, call0 + e, a.proba, a.step_size, sd, rp, P + 3 * e, pn);
-      const double u = a.proposals ? a.uniforms[((int64_t)istep * nmove + im) * nw + w]
-                                   : accept_uniform(rng, call0 + ne);
       // determinant ratio y_l, y = phi(r')^T A^-1
-      warp_ao_row<R>(t, pn[0], pn[1], pn[2], AO, lane);
-      warp_mo_row<R>(t, AO, n, PHI, lane);
+      warp_ao_row<R>(t, xt, pn[0], pn[1], pn[2], E, D, AO, lane);
+      warp_mo_row_t<R>(WT, ldt, na4, AO, n, PHI, lane);
       for (int j = lane; j < n; j += 32) {
         R y = (R)0;
         for (int k = 0; k < n; ++k) y = fma(PHI[k], Vs[k * ld + j], y);
