@@ -37,6 +37,9 @@ CONFIGS = "single_double(4,4)"
 STEP_SIZE = 0.2
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 NWALKERS = 16384
+C6H6 = ("C 1.39 0 0; C 0.695 1.20377 0; C -0.695 1.20377 0; C -1.39 0 0; "
+        "C -0.695 -1.20377 0; C 0.695 -1.20377 0; H 2.48 0 0; H 1.24 2.14774 0; "
+        "H -1.24 2.14774 0; H -2.48 0 0; H -1.24 -2.14774 0; H 1.24 -2.14774 0")
 METRIC = ("walker-steps/s (Metropolis all-electron, mixed-precision method; "
           "E_L/s and the plain FP64 method alongside)")
 
@@ -56,6 +59,9 @@ def parse():
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--nwalkers", type=int, default=16384)
+    p.add_argument("--c6h6-walkers", type=int, default=65536)
+    p.add_argument("--c6h6-sweeps", type=int, default=4,
+                   help="all-elec-iter sweeps per timed C6H6 launch (mixed method)")
     p.add_argument("--mc-steps", type=int, default=100)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
     return p.parse_args()
@@ -249,6 +255,94 @@ def precision_study(torch, wf64, wfm, x_eq, sampler, nfixed=100_000):
             "stat_error_of_mean_ha": float(e64.std() / nfixed ** 0.5)}
 
 
+def metropolis_capi(torch, lib, wf, x, nstep, move_type, step, seed, generic=False, scratch=None):
+    """qmc_metropolis_run on x (advanced in place) on the current stream;
+    generic=True requests psi_out, which selects the kernel that re-evaluates
+    psi for every move instead of the Sherman-Morrison sampler."""
+    import ctypes
+
+    from qmctorch_gb300 import _lib
+    nw = x.shape[0]
+    call = wf._desc(x.device)
+    need = lib.qmc_metropolis_scratch_bytes(call.ref, nw)
+    if scratch is None or scratch.numel() < need:
+        scratch = torch.empty(max(need, 1), dtype=torch.uint8, device=x.device)
+    psi = torch.empty(nw, dtype=torch.float64, device=x.device) if generic else None
+    a = _lib.MetropolisArgs()
+    a.pos = ctypes.c_void_p(x.data_ptr())
+    a.nwalkers, a.nstep, a.ntherm, a.ndecor = nw, nstep, nstep, 1
+    a.move_type, a.proba, a.step_size, a.seed, a.step_offset = move_type, 0, step, seed, 0
+    a.psi_out = ctypes.c_void_p(psi.data_ptr()) if generic else None
+    _lib.check(lib.qmc_metropolis_run(call.ref, a, ctypes.c_void_p(scratch.data_ptr()),
+                                      scratch.numel(),
+                                      ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
+               "qmc_metropolis_run")
+    return scratch, psi
+
+
+def bench_c6h6(torch, lib, args, device, flush, rank):
+    """C6H6 cc-pVDZ, single determinant + Pade e-e Jastrow, all-elec-iter
+    sweeps (42 single-electron moves each) with step 0.1: walker-sweeps/s of
+    the Sherman-Morrison sampler in both methods, E_L/s, and the kernel that
+    re-evaluates psi for every move on a 4096-walker subset."""
+    import ctypes
+
+    from qmctorch_gb300 import _lib
+    from qmctorch_gb300.scf import Molecule
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    mol = Molecule(C6H6, unit="angs", basis="cc-pvdz")
+    nw = args.c6h6_walkers
+    x0 = torch.as_tensor(seeded_positions(mol, nw, seed=50 + rank), device=device)
+    stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    out = {"workload": "c6h6_ccpvdz_ground_state_%dw_all_elec_iter" % nw,
+           "molecule": "C6H6 cc-pVDZ (120 cart AOs, 42 e)", "configs": "ground_state",
+           "move": "all-elec-iter (one sweep = 42 single-electron moves)", "step_size": 0.1,
+           "nwalkers": nw}
+    wfs = {}
+    for name in ("mixed", "fp64"):
+        wf = SlaterJastrow(mol, configs="ground_state", cuda=True, precision=name)
+        wfs[name] = wf
+        x = x0.clone()
+        sweeps = args.c6h6_sweeps if name == "mixed" else 1
+        steps = args.steps if name == "mixed" else max(2, args.steps // 4)
+        scr, _ = metropolis_capi(torch, lib, wf, x, 1, 2, 0.1, 11)
+        for _ in range(max(1, args.warmup if name == "mixed" else 1)):
+            metropolis_capi(torch, lib, wf, x, sweeps, 2, 0.1, 12, scratch=scr)
+        torch.cuda.synchronize()
+        t = _timed(torch, lambda i: metropolis_capi(torch, lib, wf, x, sweeps, 2, 0.1, 100 + i,
+                                                     scratch=scr), steps, flush)
+        call = wf._desc(device)
+        el_scr = torch.empty(lib.qmc_scratch_bytes(call.ref, nw, 1), dtype=torch.uint8,
+                             device=device)
+        eloc = torch.empty(nw, dtype=torch.float64, device=device)
+
+        def el_call(i):
+            _lib.check(lib.qmc_wf_local_energy(call.ref, ctypes.c_void_p(x.data_ptr()), nw,
+                                               ctypes.c_void_p(eloc.data_ptr()), None, None,
+                                               ctypes.c_void_p(el_scr.data_ptr()),
+                                               el_scr.numel(), stream), "qmc_wf_local_energy")
+        el_call(0)
+        torch.cuda.synchronize()
+        el_t = _timed(torch, el_call, 3, flush)
+        # the kernel that re-evaluates psi for every move, on a subset
+        ng = 4096
+        xg = x[:ng].clone()
+        gscr, _ = metropolis_capi(torch, lib, wf, xg, 1, 2, 0.1, 13, generic=True)
+        torch.cuda.synchronize()
+        g_t = _timed(torch, lambda i: metropolis_capi(torch, lib, wf, xg, 1, 2, 0.1, 200 + i,
+                                                       generic=True, scratch=gscr), 2, flush)
+        out[name] = {"walker_sweeps_per_s": nw * sweeps * steps / t,
+                     "ms_per_sweep": t * 1e3 / (sweeps * steps), "timed_launches": steps,
+                     "sweeps_per_launch": sweeps, "el_per_s": nw * 3 / el_t,
+                     "reevaluating_kernel_walker_sweeps_per_s": ng * 2 / g_t}
+        out[name]["speedup_vs_reevaluating_kernel"] = (
+            out[name]["walker_sweeps_per_s"] / out[name]["reevaluating_kernel_walker_sweeps_per_s"])
+    out["speedup_mixed_vs_fp64"] = {
+        "walker_sweeps": out["mixed"]["walker_sweeps_per_s"] / out["fp64"]["walker_sweeps_per_s"],
+        "el": out["mixed"]["el_per_s"] / out["fp64"]["el_per_s"]}
+    return out
+
+
 def run_gb300(args):
     import ctypes
 
@@ -330,6 +424,7 @@ def run_gb300(args):
         el_s = _timed(torch, el_call, args.steps, flush)
         results[name] = {"met_s": met_s, "el_s": el_s,
                          "accept": float(acc.sum()) / (nw * args.mc_steps * args.steps)}
+    c6h6 = bench_c6h6(torch, lib, args, device, flush, rank) if args.c6h6_walkers > 0 else None
     clk = clocks.stop()
 
     prec = precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank)) if rank == 0 else None
@@ -397,6 +492,7 @@ def run_gb300(args):
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "api": "Metropolis.__call__(wf.pdf, pos=pinned host tensor) -> host samples "
                            "(mixed method)"},
+            "c6h6_single_electron": c6h6,
             "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }
