@@ -60,6 +60,9 @@ def parse():
     p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     p.add_argument("--nwalkers", type=int, default=16384)
     p.add_argument("--c6h6-walkers", type=int, default=65536)
+    p.add_argument("--serve-requests", type=int, default=48)
+    p.add_argument("--serve-rates", type=float, nargs="*", default=[10.0, 40.0, 160.0])
+    p.add_argument("--serve-budget-gb", type=int, default=32)
     p.add_argument("--c6h6-sweeps", type=int, default=4,
                    help="all-elec-iter sweeps per timed C6H6 launch (mixed method)")
     p.add_argument("--mc-steps", type=int, default=100)
@@ -343,6 +346,34 @@ def bench_c6h6(torch, lib, args, device, flush, rank):
     return out
 
 
+def bench_serving(args):
+    """Continuous-batching single-point server on a seeded Poisson stream of
+    H_n sto-3g requests (n even in 2..32, spacing 0.7-1.2 A, walkers
+    log-uniform 1024-16384, 100-1000 steps, mixed method), at each arrival rate
+    of --serve-rates: p50 / p99 latency (arrival to result) and walker-steps/s
+    over the makespan."""
+    from qmctorch_gb300.serving import (VMCServer, latency_percentiles, poisson_stream,
+                                        replay_stream)
+    out = {"workload": "h_n_sto3g_single_point_stream", "requests_per_rate": args.serve_requests,
+           "hbm_budget_bytes": args.serve_budget_gb << 30, "slice_steps": 64, "rates": []}
+    # warm-up: build and load every shape once (kernels, plans, molecules)
+    warm = VMCServer(hbm_budget=args.serve_budget_gb << 30)
+    replay_stream(warm, poisson_stream(8, 1000.0, seed=99, smin=20, smax=20, wmin=256,
+                                       wmax=256))
+    for rate in args.serve_rates:
+        srv = VMCServer(hbm_budget=args.serve_budget_gb << 30)
+        stream = poisson_stream(args.serve_requests, rate, seed=0)
+        res, makespan = replay_stream(srv, stream)
+        ws = sum(r.nwalkers * r.nstep for r in res)
+        lat = latency_percentiles(res)
+        out["rates"].append({"lambda_per_s": rate, "completed": len(res),
+                             "p50_latency_s": lat["p50"], "p99_latency_s": lat["p99"],
+                             "walker_steps_per_s": ws / makespan, "makespan_s": makespan,
+                             "launches": srv.launches,
+                             "jobs_per_launch": srv.launched_jobs / max(srv.launches, 1)})
+    return out
+
+
 def run_gb300(args):
     import ctypes
 
@@ -426,6 +457,7 @@ def run_gb300(args):
                          "accept": float(acc.sum()) / (nw * args.mc_steps * args.steps)}
     c6h6 = bench_c6h6(torch, lib, args, device, flush, rank) if args.c6h6_walkers > 0 else None
     clk = clocks.stop()
+    serving = bench_serving(args) if (args.serve_requests > 0 and rank == 0) else None
 
     prec = precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank)) if rank == 0 else None
 
@@ -493,6 +525,7 @@ def run_gb300(args):
                     "api": "Metropolis.__call__(wf.pdf, pos=pinned host tensor) -> host samples "
                            "(mixed method)"},
             "c6h6_single_electron": c6h6,
+            "serving": serving,
             "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }

@@ -270,6 +270,33 @@ int64_t qmc_metropolis_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
 int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a,
                        void* scratch, int64_t scratch_bytes, void* stream);
 
+/*
+ * qmc_metropolis_run for up to QMC_MAX_BATCH independent jobs in one launch
+ * (no reference counterpart: the serving loop's continuous batching). Job j
+ * is (descs[j], args[j]) with its own scratch[j] of scratch_bytes[j] bytes;
+ * each job's walkers evolve exactly as in a qmc_metropolis_run call with the
+ * same arguments (bitwise), whatever the other jobs are. Jobs must share the
+ * launch shape: precision, electron count, determinant columns and table
+ * sizes (e.g. H_n chains of one n); otherwise QMC_ERR_SHAPE. All-electron
+ * moves without replay inputs or psi_out only (QMC_ERR_UNSUPPORTED).
+ */
+#define QMC_MAX_BATCH 32
+int qmc_metropolis_run_batch(const qmc_wf_desc* descs, const qmc_metropolis_args* args,
+                             void* const* scratch, const int64_t* scratch_bytes, int32_t njobs,
+                             void* stream);
+
+/*
+ * Compensated statistics of x[0..n) (local energies): stats[0] = mean,
+ * stats[1] = unbiased variance, stats[2] = sqrt(stats[1] / n). Replaces the
+ * torch.mean / torch.var / WaveFunction.sampling_error of
+ * SolverBase.single_point (solver_base.py:316-387, wf_base.py:225-229).
+ * Two passes of Neumaier-compensated sums merged in a fixed order: the result
+ * depends on n only. stats is a device pointer.
+ */
+int64_t qmc_reduce_scratch_bytes(int64_t n);
+int qmc_reduce_stats(const double* x, int64_t n, double* stats, void* scratch,
+                     int64_t scratch_bytes, void* stream);
+
 /* Human-readable status. */
 const char* qmc_status_string(int status);
 

@@ -23,7 +23,7 @@ BUILD = os.path.join(ROOT, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
-           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu"]
+           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu", "qmc_reduce.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 
@@ -136,6 +136,11 @@ SIGNATURES = {
     "qmc_probe_fma": (ctypes.c_int, [c_int32, c_int32, c_int64, c_void_p, c_void_p]),
     "qmc_metropolis_run": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), c_void_p, c_int64,
                                           c_void_p]),
+    "qmc_metropolis_run_batch": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), _P(c_void_p),
+                                                _P(c_int64), c_int32, c_void_p]),
+    "qmc_reduce_scratch_bytes": (c_int64, [c_int64]),
+    "qmc_reduce_stats": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_int64,
+                                        c_void_p]),
 }
 
 _LIB = None

@@ -6,6 +6,8 @@
 #include "qmc_host.cuh"
 #include "qmc_rng.cuh"
 
+#include <mutex>
+
 namespace qmc {
 
 // One block advances `nwb` walker chains through all steps. Per move: every
@@ -16,14 +18,14 @@ namespace qmc {
 // (seed); call = move * (nelec + 2) + e for electron e's three normals,
 // + nelec for the accept uniform, + nelec + 1 for the one-elec electron index.
 template <typename R, int JC>
-__global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const qmc_wf_desc d, const qmc_metropolis_args a,
-                                                          unsigned char* __restrict__ scr, int64_t ss,
-                                                          const EPShape S) {
-  extern __shared__ __align__(16) unsigned char smem[];
+__device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc_metropolis_args& a,
+                                                 unsigned char* __restrict__ scr, int64_t ss,
+                                                 const EPShape& S, int64_t block,
+                                                 unsigned char* smem) {
   const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
   const int64_t nw = a.nwalkers;
   const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne;
-  const int64_t w0 = (int64_t)blockIdx.x * nwb;
+  const int64_t w0 = block * nwb;
   const int tid = threadIdx.x;
   const int slot = tid / nwb, wl = tid - (tid / nwb) * nwb;
   const int nslot = S.nslot;
@@ -140,6 +142,73 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) metropolis_kernel(const 
 }
 
 template <typename R, int JC>
+__global__ void __launch_bounds__(EPBound<R>::kThreads)
+    metropolis_kernel(const __grid_constant__ qmc_wf_desc d,
+                      const __grid_constant__ qmc_metropolis_args a, unsigned char* __restrict__ scr,
+                      int64_t ss, const __grid_constant__ EPShape S) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  metropolis_block<R, JC>(d, a, scr, ss, S, blockIdx.x, smem);
+}
+
+// Several independent jobs (molecules of one launch shape: same electron
+// count and table sizes) in one launch. The job table travels in the kernel
+// parameters; block b serves job j with block0[j] <= b < block0[j + 1].
+struct MetBatchJob {
+  qmc_wf_desc d;
+  qmc_metropolis_args a;
+  unsigned char* scr;
+  int64_t ss;
+};
+struct MetBatch {
+  int32_t njobs;
+  int64_t block0[QMC_MAX_BATCH + 1];
+  MetBatchJob job[QMC_MAX_BATCH];
+};
+
+template <typename R, int JC>
+__global__ void __launch_bounds__(EPBound<R>::kThreads)
+    metropolis_batch_kernel(const __grid_constant__ MetBatch b, const __grid_constant__ EPShape S) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int64_t bid = blockIdx.x;
+  int j = 0;
+  while (j + 1 < b.njobs && b.block0[j + 1] <= bid) ++j;
+  const MetBatchJob& J = b.job[j];
+  metropolis_block<R, JC>(J.d, J.a, J.scr, J.ss, S, bid - b.block0[j], smem);
+}
+
+template <typename R, int JC>
+static int launch_metropolis_batch(const qmc_wf_desc* descs, const qmc_metropolis_args* args,
+                                   void* const* scratch, int njobs, cudaStream_t s) {
+  int64_t nwt = 0;
+  for (int j = 0; j < njobs; ++j) nwt += args[j].nwalkers;
+  const EPShape S = ep_plan<R>(descs[0], 2, JC, metropolis_batch_kernel<R, JC>, nwt);
+  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
+  for (int j = 1; j < njobs; ++j) {
+    const EPShape Sj = ep_shape<R>(descs[j], 2, S.nwb, JC, S.nslot);
+    if (Sj.smem != S.smem || Sj.o_pos != S.o_pos || Sj.o_mo != S.o_mo || Sj.o_acc != S.o_acc ||
+        Sj.ncol != S.ncol || Sj.nthreads != S.nthreads)
+      return QMC_ERR_SHAPE;
+  }
+  int st = prepare_smem(metropolis_batch_kernel<R, JC>, S.smem);
+  if (st) return st;
+  static MetBatch b;  // host staging of the parameter block (copied at launch)
+  static std::mutex mu;
+  std::lock_guard<std::mutex> g(mu);
+  b.njobs = njobs;
+  b.block0[0] = 0;
+  for (int j = 0; j < njobs; ++j) {
+    b.job[j].d = descs[j];
+    b.job[j].a = args[j];
+    b.job[j].scr = (unsigned char*)scratch[j];
+    b.job[j].ss = pad_walkers(args[j].nwalkers);
+    b.block0[j + 1] = b.block0[j] + (args[j].nwalkers + S.nwb - 1) / S.nwb;
+  }
+  if (b.block0[njobs] == 0) return QMC_OK;
+  metropolis_batch_kernel<R, JC><<<(unsigned)b.block0[njobs], S.nthreads, S.smem, s>>>(b, S);
+  return launch_status();
+}
+
+template <typename R, int JC>
 static int launch_metropolis(const qmc_wf_desc* d, const qmc_metropolis_args* a, unsigned char* scr,
                              cudaStream_t s) {
   const EPShape S = ep_plan<R>(*d, 2, JC, metropolis_kernel<R, JC>, a->nwalkers);
@@ -184,6 +253,40 @@ int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void*
   if (d->nmo_used <= 8) return launch_metropolis<double, 8>(d, a, scr, s);
   if (d->nmo_used <= 16) return launch_metropolis<double, 16>(d, a, scr, s);
   return launch_metropolis<double, 24>(d, a, scr, s);
+}
+
+int qmc_metropolis_run_batch(const qmc_wf_desc* descs, const qmc_metropolis_args* args,
+                             void* const* scratch, const int64_t* scratch_bytes, int32_t njobs,
+                             void* stream) {
+  if (njobs < 1 || njobs > QMC_MAX_BATCH || !descs || !args || !scratch || !scratch_bytes)
+    return QMC_ERR_ARG;
+  for (int j = 0; j < njobs; ++j) {
+    const qmc_wf_desc* d = descs + j;
+    const qmc_metropolis_args* a = args + j;
+    int st = check_desc(d);
+    if (st) return st;
+    if (a->nwalkers < 0 || a->nstep < 0 || a->ndecor < 1 || a->ntherm < 0 || a->proba < 0 ||
+        a->proba > 1)
+      return QMC_ERR_ARG;
+    if (a->move_type != QMC_MOVE_ALL_ELEC || a->proposals || a->psi_out)
+      return QMC_ERR_UNSUPPORTED;
+    if (a->nwalkers > 0 && (!a->pos || !scratch[j])) return QMC_ERR_ARG;
+    if (a->samples && a->nsnap < 0) return QMC_ERR_ARG;
+    if (scratch_bytes[j] < qmc_metropolis_scratch_bytes(d, a->nwalkers)) return QMC_ERR_SCRATCH;
+    if (d->precision != descs[0].precision || d->nelec != descs[0].nelec ||
+        d->nmo_used != descs[0].nmo_used)
+      return QMC_ERR_SHAPE;
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  const qmc_wf_desc* d = descs;
+  if (d->precision == QMC_PREC_MIXED) {
+    if (d->nmo_used <= 8) return launch_metropolis_batch<float, 8>(descs, args, scratch, njobs, s);
+    if (d->nmo_used <= 16) return launch_metropolis_batch<float, 16>(descs, args, scratch, njobs, s);
+    return launch_metropolis_batch<float, 24>(descs, args, scratch, njobs, s);
+  }
+  if (d->nmo_used <= 8) return launch_metropolis_batch<double, 8>(descs, args, scratch, njobs, s);
+  if (d->nmo_used <= 16) return launch_metropolis_batch<double, 16>(descs, args, scratch, njobs, s);
+  return launch_metropolis_batch<double, 24>(descs, args, scratch, njobs, s);
 }
 
 }  // extern "C"

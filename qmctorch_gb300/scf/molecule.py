@@ -131,53 +131,68 @@ def build_basis_namespace(atoms, atom_coords, basis_name):
     return basis
 
 
-def _overlap_1d(i, j, xpa, xpb, inv2p):
-    """Obara-Saika 1D overlap recursion, table up to (i, j)."""
-    s = np.zeros((i + 1, j + 1))
-    s[0, 0] = 1.0
-    for a in range(i + 1):
-        for b in range(j + 1):
+def _overlap_1d_table(kmax, xpa, xpb, inv2p):
+    """Obara-Saika 1D overlap recursion for arrays of primitive pairs:
+    table[a][b] (a, b <= kmax), each an array over the pairs."""
+    s = [[None] * (kmax + 1) for _ in range(kmax + 1)]
+    s[0][0] = np.ones_like(xpa)
+    for a in range(kmax + 1):
+        for b in range(kmax + 1):
             if a == 0 and b == 0:
                 continue
             if a > 0:
-                v = xpa * s[a - 1, b]
+                v = xpa * s[a - 1][b] if b <= kmax else None
                 if a > 1:
-                    v += inv2p * (a - 1) * s[a - 2, b]
+                    v = v + inv2p * (a - 1) * s[a - 2][b]
                 if b > 0:
-                    v += inv2p * b * s[a - 1, b - 1]
+                    v = v + inv2p * b * s[a - 1][b - 1]
             else:
-                v = xpb * s[a, b - 1]
+                v = xpb * s[a][b - 1]
                 if b > 1:
-                    v += inv2p * (b - 1) * s[a, b - 2]
-            s[a, b] = v
-    return s[i, j]
+                    v = v + inv2p * (b - 1) * s[a][b - 2]
+            s[a][b] = v
+    return s
 
 
 def ao_overlap(basis, atom_coords):
     """Overlap matrix of the AOs as evaluated by the AO layer
-    (weights c_p * N_p, entries summed by index_ctr)."""
+    (weights c_p * N_p, entries summed by index_ctr); all primitive pairs at
+    once."""
     nao = basis.nao
-    centers = np.repeat(np.asarray(atom_coords), basis.nshells, axis=0)
-    w = basis.bas_coeffs * basis.bas_norm
-    k = np.stack([basis.bas_kx, basis.bas_ky, basis.bas_kz], axis=1)
-    idx = np.asarray(basis.index_ctr)
+    centers = np.repeat(np.asarray(atom_coords, dtype=np.float64), basis.nshells, axis=0)
+    w = np.asarray(basis.bas_coeffs, dtype=np.float64) * np.asarray(basis.bas_norm)
+    k = np.stack([basis.bas_kx, basis.bas_ky, basis.bas_kz], axis=1).astype(np.int64)
+    idx = np.asarray(basis.index_ctr, dtype=np.int64)
+    ex = np.asarray(basis.bas_exp, dtype=np.float64)
+    p, q = np.triu_indices(len(w))
+    a, b = ex[p], ex[q]
+    A, B = centers[p], centers[q]
+    pp = a + b
+    P = (a[:, None] * A + b[:, None] * B) / pp[:, None]
+    dAB = (A - B) ** 2
+    r2 = -a * b / pp * ((dAB[:, 0] + dAB[:, 1]) + dAB[:, 2])
+    # scalar libm exp / pow per pair (array versions may round differently)
+    val = np.array([math.exp(x) * (math.pi / y) ** 1.5 for x, y in zip(r2.tolist(), pp.tolist())])
+    kmax = int(k.max()) if k.size else 0
+    for d in range(3):
+        tab = _overlap_1d_table(kmax, P[:, d] - A[:, d], P[:, d] - B[:, d], 0.5 / pp)
+        sd = np.empty_like(val)
+        for ka in range(kmax + 1):
+            for kb in range(kmax + 1):
+                m = (k[p, d] == ka) & (k[q, d] == kb)
+                sd[m] = tab[ka][kb][m]
+        val = val * sd
+    val = val * (w[p] * w[q])
+    # accumulate in pair order, (p, q) then (q, p), so that S is summed exactly
+    # as a loop over the pairs would
+    off = p != q
+    n = len(p)
+    rows = np.stack([idx[p], np.where(off, idx[q], -1)], axis=1).reshape(-1)
+    cols = np.stack([idx[q], np.where(off, idx[p], -1)], axis=1).reshape(-1)
+    vals = np.stack([val, val], axis=1).reshape(-1)
+    keep = rows >= 0
     S = np.zeros((nao, nao))
-    npr = len(w)
-    for p in range(npr):
-        for q in range(p, npr):
-            a, b = basis.bas_exp[p], basis.bas_exp[q]
-            A, B = centers[p], centers[q]
-            pp = a + b
-            P = (a * A + b * B) / pp
-            kab = math.exp(-a * b / pp * float(np.sum((A - B) ** 2)))
-            val = kab * (math.pi / pp) ** 1.5
-            for d in range(3):
-                val *= _overlap_1d(int(k[p, d]), int(k[q, d]), P[d] - A[d], P[d] - B[d],
-                                   0.5 / pp)
-            val *= w[p] * w[q]
-            S[idx[p], idx[q]] += val
-            if q != p:
-                S[idx[q], idx[p]] += val
+    np.add.at(S, (rows[keep], cols[keep]), vals[keep])
     return S
 
 

@@ -1,0 +1,414 @@
+"""Continuous-batching VMC single-point server on one GPU.
+
+The reference has no serving layer; its unit of work is
+``Solver.single_point()`` (solver_base.py:316-387): sample the wave function
+with Metropolis, evaluate the local energy on the kept walkers, report mean,
+variance and sampling error. A request here is one such single point
+(``nstep`` all-electron Metropolis steps from seeded positions, the last
+positions kept as with the sampler's default ``ntherm = -1``), for any
+molecule the kernels support.
+
+Scheduling (``Scheduler``):
+
+* requests queue FIFO and are admitted while their device footprint
+  (positions, Metropolis scratch, local-energy scratch and outputs) fits the
+  HBM budget and an active slot is free; a request that does not fit waits
+  at the head of the queue;
+* every admitted job's walker state stays resident on the device until it
+  retires;
+* the sampling work is cut into slices of ``slice_steps`` steps. Each
+  scheduler pass gathers the jobs whose previous slice has finished, groups
+  them by launch shape (electron count, table sizes, precision) and issues
+  one ``qmc_metropolis_run_batch`` launch per group of up to ``QMC_MAX_BATCH``
+  jobs, on a pool of CUDA streams, so groups overlap on the device and a job
+  admitted while others run joins the next launch of its group;
+* a job whose steps are done gets its local energies and compensated
+  statistics (``qmc_reduce_stats``) on its stream, and retires when they are
+  ready, releasing its budget.
+
+Each walker's random stream is keyed by (seed, walker, step) and every
+kernel's per-walker arithmetic is independent of the launch it runs in, so a
+request's result is bitwise the same alone and in any mix.
+
+The executor (device work) is separate from the scheduler so that the
+scheduling logic is testable without a GPU.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import time
+from collections import deque
+from dataclasses import dataclass, field
+
+import numpy as np
+
+MAX_BATCH = 32  # QMC_MAX_BATCH of qmc_metropolis_run_batch
+
+
+@dataclass
+class Request:
+    """One VMC single point: ``atoms`` (``Molecule`` syntax), ``nwalkers``
+    walkers, ``nstep`` all-electron Metropolis steps of ``step_size``."""
+    atoms: str
+    nwalkers: int
+    nstep: int
+    unit: str = "angs"
+    basis: str = "sto-3g"
+    configs: str = "ground_state"
+    step_size: float = 0.2
+    seed: int = 0
+    precision: str = "mixed"
+    rid: int = -1
+    arrival: float = 0.0
+
+
+@dataclass
+class Result:
+    rid: int
+    energy: float
+    variance: float
+    error: float
+    nwalkers: int
+    nstep: int
+    arrival: float
+    admitted: float
+    done: float
+
+    @property
+    def latency(self):
+        return self.done - self.arrival
+
+
+@dataclass
+class _Job:
+    req: Request
+    key: tuple
+    footprint: int
+    admitted: float
+    steps_done: int = 0
+    inflight: object = None      # token of the slice or energy work in flight
+    phase: str = "sampling"      # sampling -> energy -> (retired)
+    handle: object = None        # executor state
+    order: int = 0
+
+
+class Scheduler:
+    """FIFO admission under an HBM budget, slice-wise batched sampling,
+    energy evaluation and retirement. ``executor`` provides the device work."""
+
+    def __init__(self, executor, hbm_budget, max_active=256, slice_steps=64, nstreams=4,
+                 clock=time.perf_counter):
+        self.ex = executor
+        self.budget = int(hbm_budget)
+        self.max_active = max_active
+        self.slice_steps = slice_steps
+        self.nstreams = nstreams
+        self.clock = clock
+        self.queue = deque()
+        self.active = []
+        self.used = 0
+        self.next_rid = 0
+        self.results = {}
+        self._stream_rr = 0
+        self._order = 0
+        self.launches = 0       # batched Metropolis launches
+        self.launched_jobs = 0  # job slices in them
+
+    # -- public API -------------------------------------------------------
+    def submit(self, req):
+        req.rid = self.next_rid
+        self.next_rid += 1
+        req.arrival = self.clock()
+        fp = self.ex.footprint(req)
+        if fp > self.budget:
+            raise ValueError("request %d needs %d bytes, more than the HBM budget %d"
+                             % (req.rid, fp, self.budget))
+        self.queue.append((req, fp))
+        return req.rid
+
+    def idle(self):
+        return not self.queue and not self.active
+
+    def poll(self):
+        """One scheduler pass; returns the results retired in it."""
+        done = self._retire()
+        self._admit()
+        self._launch()
+        return done
+
+    def run(self, sleep=2e-4):
+        """Poll until every submitted request has a result."""
+        out = []
+        while not self.idle():
+            got = self.poll()
+            out += got
+            if not got:
+                time.sleep(sleep)
+        return out
+
+    # -- internals --------------------------------------------------------
+    def _stream(self):
+        s = self._stream_rr
+        self._stream_rr = (self._stream_rr + 1) % self.nstreams
+        return s
+
+    def _retire(self):
+        out = []
+        keep = []
+        for job in self.active:
+            if job.inflight is not None and self.ex.ready(job.inflight):
+                job.inflight = None
+                if job.phase == "energy":
+                    e, v, err = self.ex.stats(job.handle)
+                    r = Result(job.req.rid, e, v, err, job.req.nwalkers, job.req.nstep,
+                               job.req.arrival, job.admitted, self.clock())
+                    self.results[r.rid] = r
+                    out.append(r)
+                    self.ex.release(job.handle)
+                    self.used -= job.footprint
+                    continue
+            keep.append(job)
+        self.active = keep
+        # jobs whose sampling finished go to the energy phase
+        for job in self.active:
+            if job.phase == "sampling" and job.inflight is None and job.steps_done >= job.req.nstep:
+                job.phase = "energy"
+                job.inflight = self.ex.launch_energy(job.handle, self._stream())
+        return out
+
+    def _admit(self):
+        while self.queue and len(self.active) < self.max_active:
+            req, fp = self.queue[0]
+            if self.used + fp > self.budget:
+                break
+            self.queue.popleft()
+            handle, key = self.ex.admit(req)
+            self.used += fp
+            self._order += 1
+            self.active.append(_Job(req, key, fp, self.clock(), handle=handle, order=self._order))
+
+    def _launch(self):
+        ready = {}
+        for job in self.active:
+            if job.phase == "sampling" and job.inflight is None and job.steps_done < job.req.nstep:
+                ready.setdefault(job.key, []).append(job)
+        for key, jobs in ready.items():
+            jobs.sort(key=lambda j: j.order)
+            for i in range(0, len(jobs), MAX_BATCH):
+                chunk = jobs[i:i + MAX_BATCH]
+                steps = [min(self.slice_steps, j.req.nstep - j.steps_done) for j in chunk]
+                token = self.ex.launch_slice([j.handle for j in chunk],
+                                             [j.steps_done for j in chunk], steps, self._stream())
+                self.launches += 1
+                self.launched_jobs += len(chunk)
+                for j, n in zip(chunk, steps):
+                    j.steps_done += n
+                    j.inflight = token
+
+
+def hydrogen_chain(n, spacing):
+    """Linear H_n along z with the given spacing (angstrom), ``Molecule`` syntax."""
+    return "; ".join("H 0 0 %.10f" % (i * spacing) for i in range(n))
+
+
+def seeded_positions(mol, nw, seed):
+    """Electrons on their atoms (in ``atomic_nelec`` order) with N(0, 1 bohr^2)
+    offsets per coordinate, seeded."""
+    rng = np.random.default_rng(seed)
+    centers = np.repeat(np.asarray(mol.atom_coords), mol.atomic_nelec, axis=0)[: mol.nelec]
+    return (centers[None] + rng.normal(size=(nw, mol.nelec, 3))).reshape(nw, -1)
+
+
+class GPUExecutor:
+    """Device work of the scheduler: wave functions, resident walker state,
+    batched Metropolis slices, local energies and statistics."""
+
+    def __init__(self, device=None, nstreams=4):
+        import torch
+
+        from . import _lib
+        from .wavefunction import runtime as rt
+        self.torch = torch
+        self.lib = _lib.lib()
+        self._lib = _lib
+        self.rt = rt
+        self.device = device or rt.cuda_device()
+        self.streams = [torch.cuda.Stream(device=self.device) for _ in range(nstreams)]
+        self._mols = {}
+        self._sizes = {}
+
+    def _molecule(self, req):
+        from .scf import Molecule
+        k = (req.atoms, req.unit, req.basis)
+        if k not in self._mols:
+            self._mols[k] = Molecule(req.atoms, unit=req.unit, basis=req.basis)
+            if len(self._mols) > 4096:
+                self._mols.clear()
+        return self._mols[k]
+
+    def _wf(self, req, mol):
+        from .wavefunction import SlaterJastrow
+        self.torch.set_default_dtype(self.torch.float64)
+        return SlaterJastrow(mol, configs=req.configs, cuda=True, precision=req.precision)
+
+    def _shape_key(self, req, mol):
+        return (mol.nelec, mol.nup, mol.basis.nao, len(mol.atoms), req.basis, req.configs,
+                req.precision)
+
+    def footprint(self, req):
+        mol = self._molecule(req)
+        k = self._shape_key(req, mol)
+        if k not in self._sizes:
+            wf = self._wf(req, mol)
+            call = wf._desc(self.device)
+            self._sizes[k] = (call, wf)
+        call, _ = self._sizes[k]
+        nw = req.nwalkers
+        return int(nw * 3 * mol.nelec * 8                      # positions
+                   + self.lib.qmc_metropolis_scratch_bytes(call.ref, nw)
+                   + self.lib.qmc_scratch_bytes(call.ref, nw, 1)  # local energy
+                   + nw * 8 + self.lib.qmc_reduce_scratch_bytes(nw) + 64)
+
+    def admit(self, req):
+        torch = self.torch
+        mol = self._molecule(req)
+        wf = self._wf(req, mol)
+        call = wf._desc(self.device)
+        nw = req.nwalkers
+        x = torch.as_tensor(seeded_positions(mol, nw, req.seed), device=self.device)
+        h = {
+            "req": req, "wf": wf, "call": call, "x": x,
+            "met_scr": self.rt.scratch(self.lib.qmc_metropolis_scratch_bytes(call.ref, nw),
+                                       self.device),
+            "el_scr": self.rt.scratch(self.lib.qmc_scratch_bytes(call.ref, nw, 1), self.device),
+            "eloc": torch.empty(nw, dtype=torch.float64, device=self.device),
+            "red_scr": self.rt.scratch(self.lib.qmc_reduce_scratch_bytes(nw), self.device),
+            "stats": torch.empty(3, dtype=torch.float64, device=self.device),
+        }
+        # positions are written on the default stream; the pool streams wait for them
+        h["ready"] = torch.cuda.Event()
+        h["ready"].record(torch.cuda.current_stream(self.device))
+        return h, self._shape_key(req, mol)
+
+    def _args(self, h, offset, nstep):
+        a = self._lib.MetropolisArgs()
+        req = h["req"]
+        a.pos = self.rt.ptr(h["x"])
+        a.nwalkers = req.nwalkers
+        a.nstep = nstep
+        a.ntherm = nstep
+        a.ndecor = 1
+        a.move_type = 0
+        a.proba = 0
+        a.step_size = req.step_size
+        a.seed = req.seed
+        a.step_offset = offset
+        return a
+
+    def launch_slice(self, handles, offsets, steps, sid):
+        torch = self.torch
+        n = len(handles)
+        descs = (self._lib.WfDesc * n)(*[h["call"].desc for h in handles])
+        args = (self._lib.MetropolisArgs * n)(*[self._args(h, o, s)
+                                                for h, o, s in zip(handles, offsets, steps)])
+        scr = (ctypes.c_void_p * n)(*[h["met_scr"].data_ptr() for h in handles])
+        nb = (ctypes.c_int64 * n)(*[h["met_scr"].numel() for h in handles])
+        stream = self.streams[sid]
+        for h in handles:
+            stream.wait_event(h["ready"])
+        self._lib.check(self.lib.qmc_metropolis_run_batch(descs, args, scr, nb, n,
+                                                          ctypes.c_void_p(stream.cuda_stream)),
+                        "qmc_metropolis_run_batch")
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        for h in handles:
+            h["ready"] = ev
+        return ev
+
+    def launch_energy(self, h, sid):
+        torch = self.torch
+        stream = self.streams[sid]
+        stream.wait_event(h["ready"])
+        nw = h["req"].nwalkers
+        cs = ctypes.c_void_p(stream.cuda_stream)
+        self._lib.check(self.lib.qmc_wf_local_energy(
+            h["call"].ref, self.rt.ptr(h["x"]), nw, self.rt.ptr(h["eloc"]), None, None,
+            self.rt.ptr(h["el_scr"]), h["el_scr"].numel(), cs), "qmc_wf_local_energy")
+        self._lib.check(self.lib.qmc_reduce_stats(
+            self.rt.ptr(h["eloc"]), nw, self.rt.ptr(h["stats"]), self.rt.ptr(h["red_scr"]),
+            h["red_scr"].numel(), cs), "qmc_reduce_stats")
+        h["host_stats"] = torch.empty(3, dtype=torch.float64, pin_memory=True)
+        with torch.cuda.stream(stream):
+            h["host_stats"].copy_(h["stats"], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        h["ready"] = ev
+        return ev
+
+    def ready(self, token):
+        return token.query()
+
+    def stats(self, h):
+        return tuple(float(v) for v in h["host_stats"].tolist())
+
+    def release(self, h):
+        h.clear()
+
+
+class VMCServer(Scheduler):
+    """The scheduler with the GPU executor: ``submit(Request)``, then
+    ``poll()`` / ``run()``; ``results`` maps request ids to ``Result``."""
+
+    def __init__(self, hbm_budget=16 << 30, max_active=256, slice_steps=64, nstreams=4,
+                 device=None):
+        super().__init__(GPUExecutor(device=device, nstreams=nstreams), hbm_budget,
+                         max_active=max_active, slice_steps=slice_steps, nstreams=nstreams)
+
+
+def single_point(req, device=None):
+    """One request alone (no other job on the device)."""
+    srv = VMCServer(device=device, nstreams=1)
+    srv.submit(req)
+    return srv.run()[0]
+
+
+def poisson_stream(nreq, rate, seed=0, nmin=2, nmax=32, wmin=1024, wmax=16384, smin=100,
+                   smax=1000, precision="mixed"):
+    """Seeded request stream: linear H_n chains (n even in [nmin, nmax],
+    spacing uniform in 0.7-1.2 angstrom, sto-3g), walkers log-uniform in
+    [wmin, wmax], steps uniform in [smin, smax], Poisson arrival times of the
+    given rate (requests/s). Returns [(arrival_s, Request)]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, size=nreq))
+    out = []
+    for i in range(nreq):
+        n = int(rng.integers(nmin // 2, nmax // 2 + 1)) * 2
+        spacing = float(rng.uniform(0.7, 1.2))
+        nw = int(round(math.exp(rng.uniform(math.log(wmin), math.log(wmax)))))
+        nstep = int(rng.integers(smin, smax + 1))
+        out.append((float(t[i]), Request(atoms=hydrogen_chain(n, spacing), nwalkers=nw,
+                                         nstep=nstep, seed=1000 + i, precision=precision)))
+    return out
+
+
+def replay_stream(server, stream, clock=time.perf_counter, sleep=2e-4):
+    """Submit the requests of ``stream`` at their arrival times (seconds from
+    now) while polling ``server``; returns (results, makespan_s)."""
+    t0 = clock()
+    pending = list(stream)
+    out = []
+    while pending or not server.idle():
+        now = clock() - t0
+        while pending and pending[0][0] <= now:
+            server.submit(pending.pop(0)[1])
+        got = server.poll()
+        out += got
+        if not got:
+            time.sleep(sleep)
+    return out, clock() - t0
+
+
+def latency_percentiles(results, q=(50, 99)):
+    lat = np.asarray([r.latency for r in results])
+    return {"p%d" % p: float(np.percentile(lat, p)) for p in q}

@@ -17,6 +17,7 @@ import numpy as np
 import torch
 
 from ..utils import DataLoader
+from ..wavefunction import runtime as rt
 from .loss import Loss
 
 log = logging.getLogger("qmctorch_gb300")
@@ -129,7 +130,8 @@ class SolverBase:
                 chunks = [self.wf.local_energy(pos[i:i + batchsize])
                           for i in range(0, len(pos), batchsize)]
                 eloc = torch.cat(chunks)
-            e, s, err = torch.mean(eloc), torch.var(eloc), self.wf.sampling_error(eloc)
+            # mean, variance and sampling error: compensated device reduction
+            e, s, err = rt.walker_stats(eloc)
         log.info("  Energy   : %f +/- %f", e.item(), err.item())
         log.info("  Variance : %f", s.item())
         log.info("  Size     : %d", len(eloc))

@@ -55,6 +55,21 @@ def scratch(nbytes, device):
     return torch.empty(max(int(nbytes), 8), dtype=torch.uint8, device=device)
 
 
+def walker_stats(eloc):
+    """(mean, unbiased variance, sqrt(variance / n)) of the local energies by
+    the compensated qmc_reduce_stats kernel; returned on eloc's device."""
+    device = cuda_device()
+    x = dev64(eloc.reshape(-1), device)
+    n = x.numel()
+    lib = _lib.lib()
+    scr = scratch(lib.qmc_reduce_scratch_bytes(n), device)
+    out = torch.empty(3, dtype=F64, device=device)
+    _lib.check(lib.qmc_reduce_stats(ptr(x), n, ptr(out), ptr(scr), scr.numel(), stream_handle()),
+               "qmc_reduce_stats")
+    out = out.to(device=eloc.device, dtype=eloc.dtype)
+    return out[0], out[1], out[2]
+
+
 class Call:
     """A filled ``qmc_wf_desc`` plus the tensors its pointers refer to."""
 
