@@ -346,6 +346,86 @@ def bench_c6h6(torch, lib, args, device, flush, rank):
     return out
 
 
+def bench_h2_lih(torch, device):
+    """The reference's small configurations through the public API (plain
+    FP64 method): H2 sto-3g Solver.single_point (4096 walkers, 500 steps,
+    200 burn-in, every later step kept: 1.23 M samples) and LiH sto-3g
+    cas(2,2) Solver.run (8192 walkers, 50 epochs, Adam lr 1e-3, manual
+    gradient through the hand-written adjoint, 25-step resampling)."""
+    from qmctorch_gb300.sampler import Metropolis
+    from qmctorch_gb300.scf import Molecule
+    from qmctorch_gb300.solver import Solver
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    out = {}
+    mol = Molecule("H 0 0 -0.37; H 0 0 0.37", unit="angs", basis="sto-3g")
+    wf = SlaterJastrow(mol, configs="ground_state", cuda=True, precision="fp64")
+    smp = Metropolis(nwalkers=4096, nstep=500, step_size=0.2, ntherm=200, ndecor=1, nelec=2,
+                     init=mol.domain("atomic"), cuda=True, seed=5)
+    solver = Solver(wf=wf, sampler=smp)
+    solver.single_point(with_tqdm=False)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    obs = solver.single_point(with_tqdm=False)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    out["h2_single_point"] = {
+        "workload": "h2_sto3g_4096w_500steps_single_point", "wall_s": dt,
+        "walker_steps_per_s": 4096 * 500 / dt, "samples": int(obs.local_energy.numel()),
+        "energy": float(obs.energy), "error": float(obs.error)}
+    mol = Molecule("Li 0 0 0; H 0 0 1.595", unit="angs", basis="sto-3g")
+    wf = SlaterJastrow(mol, configs="cas(2,2)", cuda=True, precision="fp64")
+    smp = Metropolis(nwalkers=8192, nstep=200, step_size=0.2, nelec=mol.nelec,
+                     init=mol.domain("atomic"), cuda=True, seed=6)
+    opt = torch.optim.Adam(wf.parameters(), lr=1e-3)
+    solver = Solver(wf=wf, sampler=smp, optimizer=opt)
+    solver.run(2)  # warm-up
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    obs = solver.run(50)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    e = [float(v) for v in obs.energy]
+    out["lih_run"] = {"workload": "lih_sto3g_cas22_8192w_50_epochs", "wall_s": dt,
+                      "epochs_per_s": 50 / dt, "energy_first": e[0], "energy_last": e[-1]}
+    return out
+
+
+def bench_staged(torch, wf, x, flush):
+    """The module kernels a caller of a single layer gets (wf.ao, wf.mo,
+    wf.jastrow; FP64, reference tensor layouts) on the bench walkers:
+    time per call and achieved HBM bandwidth of the bytes they must move
+    (positions in, the layer's output tensors out)."""
+    peak = 6800.0
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f).get("hbm_gbs", peak))
+    except Exception:
+        pass
+    nw, nc = x.shape
+    ne = nc // 3
+    out = {}
+    with torch.no_grad():
+        ao = wf.ao(x)
+        nao = ao.shape[-1]
+        nmo = wf.mo(ao).shape[-1]
+        cases = {
+            "ao_values": (lambda: wf.ao(x), nw * nc * 8 + nw * ne * nao * 8),
+            "ao_values_grad_lap": (lambda: wf.ao(x, derivative=[0, 1, 2], sum_grad=False),
+                                   nw * nc * 8 + nw * ne * nao * 8 * 5),
+            "mo_from_ao": (lambda: wf.mo(ao), nw * ne * nao * 8 + nw * ne * nmo * 8),
+            "jastrow_value_grad_lap": (lambda: wf.jastrow(x, derivative=[0, 1, 2], sum_grad=False),
+                                       nw * nc * 8 + nw * 8 + nw * 3 * ne * 8 + nw * ne * 8),
+        }
+        for name, (fn, nbytes) in cases.items():
+            fn()
+            torch.cuda.synchronize()
+            t = _timed(torch, lambda i: fn(), 5, flush) / 5
+            out[name] = {"ms": t * 1e3, "algorithmic_bytes": nbytes,
+                         "achieved_gbs": nbytes / t / 1e9, "frac_of_hbm": nbytes / t / 1e9 / peak}
+    out["hbm_peak_gbs"] = peak
+    return out
+
+
 def bench_serving(args):
     """Continuous-batching single-point server on a seeded Poisson stream of
     H_n sto-3g requests (n even in 2..32, spacing 0.7-1.2 A, walkers
@@ -355,7 +435,7 @@ def bench_serving(args):
     from qmctorch_gb300.serving import (VMCServer, latency_percentiles, poisson_stream,
                                         replay_stream)
     out = {"workload": "h_n_sto3g_single_point_stream", "requests_per_rate": args.serve_requests,
-           "hbm_budget_bytes": args.serve_budget_gb << 30, "slice_steps": 64, "rates": []}
+           "hbm_budget_bytes": args.serve_budget_gb << 30, "slice_steps": 256, "rates": []}
     # warm-up: build and load every shape once (kernels, plans, molecules)
     warm = VMCServer(hbm_budget=args.serve_budget_gb << 30)
     replay_stream(warm, poisson_stream(8, 1000.0, seed=99, smin=20, smax=20, wmin=256,
@@ -458,6 +538,8 @@ def run_gb300(args):
     c6h6 = bench_c6h6(torch, lib, args, device, flush, rank) if args.c6h6_walkers > 0 else None
     clk = clocks.stop()
     serving = bench_serving(args) if (args.serve_requests > 0 and rank == 0) else None
+    small = bench_h2_lih(torch, device) if rank == 0 else None
+    staged = bench_staged(torch, wf64, x_eq, flush) if rank == 0 else None
 
     prec = precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank)) if rank == 0 else None
 
@@ -526,6 +608,8 @@ def run_gb300(args):
                            "(mixed method)"},
             "c6h6_single_electron": c6h6,
             "serving": serving,
+            "small_configs": small,
+            "module_kernels": staged,
             "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }

@@ -360,7 +360,7 @@ class VMCServer(Scheduler):
     """The scheduler with the GPU executor: ``submit(Request)``, then
     ``poll()`` / ``run()``; ``results`` maps request ids to ``Result``."""
 
-    def __init__(self, hbm_budget=16 << 30, max_active=256, slice_steps=64, nstreams=4,
+    def __init__(self, hbm_budget=16 << 30, max_active=256, slice_steps=256, nstreams=4,
                  device=None):
         super().__init__(GPUExecutor(device=device, nstreams=nstreams), hbm_budget,
                          max_active=max_active, slice_steps=slice_steps, nstreams=nstreams)
