@@ -225,6 +225,24 @@ int qmc_wf_psi_adjoint(const qmc_wf_desc* d, const double* pos, int64_t nwalkers
                        double* grad_exp, double* grad_W, int32_t ldw, double* grad_jastrow_w,
                        double* grad_ci, void* scratch, int64_t scratch_bytes, void* stream);
 
+/* Scratch bytes for qmc_wf_local_energy_adjoint. */
+int64_t qmc_eloc_adjoint_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
+
+/*
+ * Adjoint of the local energy (FP64, AO values and derivatives recomputed):
+ * accumulates sum_w gout[w] d E_L(w) / d theta into the same outputs as
+ * qmc_wf_psi_adjoint (grad_exp per basis entry, grad_W for
+ * W = mo_scf * mo_modifier, grad_jastrow_w, grad_ci). The positions are held
+ * fixed. Replaces the autograd backward of WaveFunction.local_energy
+ * (wf_base.py:184-215 with kinetic_energy_jacobi, slater_jastrow.py:312-344)
+ * that Solver.evaluate_grad_auto runs with loss.backward() (solver.py:352-370).
+ */
+int qmc_wf_local_energy_adjoint(const qmc_wf_desc* d, const double* pos, int64_t nwalkers,
+                                const double* gout, const int32_t* weight_entry,
+                                int32_t nentries, double* grad_exp, double* grad_W, int32_t ldw,
+                                double* grad_jastrow_w, double* grad_ci, void* scratch,
+                                int64_t scratch_bytes, void* stream);
+
 /* Metropolis move types (Metropolis.configure_move, metropolis.py:179-225). */
 #define QMC_MOVE_ALL_ELEC 0
 #define QMC_MOVE_ONE_ELEC 1

@@ -133,6 +133,11 @@ SIGNATURES = {
     "qmc_wf_psi_adjoint": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                           c_int32, c_void_p, c_void_p, c_int32, c_void_p,
                                           c_void_p, c_void_p, c_int64, c_void_p]),
+    "qmc_eloc_adjoint_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
+    "qmc_wf_local_energy_adjoint": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p,
+                                                   c_void_p, c_int32, c_void_p, c_void_p, c_int32,
+                                                   c_void_p, c_void_p, c_void_p, c_int64,
+                                                   c_void_p]),
     "qmc_probe_fma": (ctypes.c_int, [c_int32, c_int32, c_int64, c_void_p, c_void_p]),
     "qmc_metropolis_run": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), c_void_p, c_int64,
                                           c_void_p]),

@@ -213,6 +213,338 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
   if (threadIdx.x == 0 && g_jw) atomicAdd(g_jw, accJ[0]);
 }
 
+
+// ---------------------------------------------------------------------------
+// Adjoint of the local energy
+// ---------------------------------------------------------------------------
+// E_L = KE + V, KE = sum_k c_k D_k T_k / sum_k c_k D_k with D_k = D_up D_down
+// of configuration k, T_k = Tr(A_up^-1 B_up) + Tr(A_down^-1 B_down) and
+// B = -1/2 (lap MO + 2 grad(U) . grad MO + (lap U + |grad U|^2) MO),
+// U = log J (slater_jastrow.py:312-344, 449-482). V does not depend on the
+// parameters. Per unique spin determinant with explicit columns (X = A_u^-1):
+//   dKE/dA_u = dD_u D_u X^T - dT_u (X B_u X)^T,   dKE/dB_u = dT_u X^T,
+// then through B to the MO values, gradients and laplacians, to W and (with
+// the primitive-level exponent derivatives of value, gradient and laplacian,
+// norms fixed) to the exponents, and through grad U, lap U to the Pade weight.
+struct ElAdjLayout {  // per-walker scratch, in doubles (item-major)
+  int64_t aov, aox, aoy, aoz, aol, ma, mx, my, mz, ml, b, ga, gb, lu, x, y, z, dv, tv, gj, lj,
+      dgw, dlw, total;
+};
+
+__host__ __device__ inline ElAdjLayout el_adj_layout(const qmc_wf_desc& d) {
+  ElAdjLayout L;
+  const int64_t ne = d.nelec, nao = d.nao, nmu = d.nmo_used;
+  const int64_t nmax = d.nup > d.ndown ? d.nup : d.ndown, nd = d.ndet[0] + d.ndet[1];
+  int64_t o = 0;
+  auto take = [&](int64_t n) {
+    const int64_t r = o;
+    o += n;
+    return r;
+  };
+  L.aov = take(ne * nao);
+  L.aox = take(ne * nao);
+  L.aoy = take(ne * nao);
+  L.aoz = take(ne * nao);
+  L.aol = take(ne * nao);
+  L.ma = take(ne * nmu);
+  L.mx = take(ne * nmu);
+  L.my = take(ne * nmu);
+  L.mz = take(ne * nmu);
+  L.ml = take(ne * nmu);
+  L.b = take(ne * nmu);
+  L.ga = take(ne * nmu);
+  L.gb = take(ne * nmu);
+  L.lu = take(nmax * nmax);
+  L.x = take(nmax * nmax);
+  L.y = take(nmax * nmax);
+  L.z = take(nmax * nmax);
+  L.dv = take(nd);
+  L.tv = take(nd);
+  L.gj = take(3 * ne);
+  L.lj = take(ne);
+  L.dgw = take(3 * ne);
+  L.dlw = take(ne);
+  L.total = o;
+  return L;
+}
+
+__global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
+    const qmc_wf_desc d, const double* __restrict__ pos, int64_t nw, const double* __restrict__ gout,
+    const int* __restrict__ w_entry, int nent, double* __restrict__ g_exp,
+    double* __restrict__ g_W, int ldw, double* __restrict__ g_jw, double* __restrict__ g_ci,
+    double* __restrict__ scr, int64_t ss) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ncol = round_up(d.nmo_used, 8);
+  const Tables<double> t = load_tables<double>(d, d.nmo_used, ncol, smem);
+  double* acc = reinterpret_cast<double*>(smem + ((tables_smem_bytes<double>(d, ncol) + 15) & ~15));
+  const int nmu = d.nmo_used, ne = d.nelec, nao = d.nao;
+  double* accW = acc;               // [nao][nmu]
+  double* accE = accW + nao * nmu;  // [nent]
+  double* accC = accE + nent;       // [ncfg]
+  double* accJ = accC + d.ncfg;     // [1]
+  const int64_t nacc = adj_acc_doubles(d, nent);
+  for (int64_t i = threadIdx.x; i < nacc; i += blockDim.x) acc[i] = 0.0;
+  __syncthreads();
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w < nw) {
+    const double gw = gout[w];
+    const ElAdjLayout L = el_adj_layout(d);
+    double* sw = scr + w;
+    auto R2 = [&](int64_t base, int e, int k, int n) -> double& {
+      return sw[(base + (int64_t)e * n + k) * ss];
+    };
+    auto AV = [&](int e, int a) -> double& { return R2(L.aov, e, a, nao); };
+    auto AX = [&](int e, int a) -> double& { return R2(L.aox, e, a, nao); };
+    auto AY = [&](int e, int a) -> double& { return R2(L.aoy, e, a, nao); };
+    auto AZ = [&](int e, int a) -> double& { return R2(L.aoz, e, a, nao); };
+    auto AL = [&](int e, int a) -> double& { return R2(L.aol, e, a, nao); };
+    auto MA = [&](int e, int j) -> double& { return R2(L.ma, e, j, nmu); };
+    auto MX = [&](int e, int j) -> double& { return R2(L.mx, e, j, nmu); };
+    auto MY = [&](int e, int j) -> double& { return R2(L.my, e, j, nmu); };
+    auto MZ = [&](int e, int j) -> double& { return R2(L.mz, e, j, nmu); };
+    auto ML = [&](int e, int j) -> double& { return R2(L.ml, e, j, nmu); };
+    auto BK = [&](int e, int j) -> double& { return R2(L.b, e, j, nmu); };
+    auto GA = [&](int e, int j) -> double& { return R2(L.ga, e, j, nmu); };
+    auto GB = [&](int e, int j) -> double& { return R2(L.gb, e, j, nmu); };
+    auto GJ = [&](int e, int x) -> double& { return R2(L.gj, e, x, 3); };
+    auto LJ = [&](int e) -> double& { return sw[(L.lj + e) * ss]; };
+    auto DGW = [&](int e, int x) -> double& { return R2(L.dgw, e, x, 3); };
+    auto DLW = [&](int e) -> double& { return sw[(L.dlw + e) * ss]; };
+    const PosView P{pos + w * 3 * ne, 1};
+    // Jastrow: grad U, lap U + |grad U|^2 per electron and their w-derivatives
+    // (K = w0 r / (1 + w r), K' = w0 / (1 + w r)^2, K'' = -2 w w0 / (1 + w r)^3)
+    const double wj = __ldg(d.jastrow_w);
+    for (int i = 0; i < ne; ++i) {
+      double g[3] = {0.0, 0.0, 0.0}, dg[3] = {0.0, 0.0, 0.0}, lap = 0.0, dlap = 0.0;
+      if (d.use_jastrow)
+        for (int j = 0; j < ne; ++j) {
+          if (j == i) continue;
+          const double dx[3] = {P(3 * i) - P(3 * j), P(3 * i + 1) - P(3 * j + 1),
+                                P(3 * i + 2) - P(3 * j + 2)};
+          const double r = sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+          const double w0 = same_spin(d, i, j) ? 0.25 : 0.5;
+          const double u = 1.0 / (1.0 + wj * r), u2 = u * u, u3 = u2 * u;
+          const double k1 = w0 * u2, k2 = -2.0 * wj * w0 * u3;
+          const double dk1 = -2.0 * w0 * r * u3, dk2 = -2.0 * w0 * u3 + 6.0 * w0 * wj * r * u3 * u;
+          for (int x = 0; x < 3; ++x) {
+            g[x] += k1 * dx[x] / r;
+            dg[x] += dk1 * dx[x] / r;
+          }
+          lap += 2.0 * k1 / r + k2;
+          dlap += 2.0 * dk1 / r + dk2;
+        }
+      for (int x = 0; x < 3; ++x) {
+        GJ(i, x) = g[x];
+        DGW(i, x) = dg[x];
+      }
+      LJ(i) = lap + g[0] * g[0] + g[1] * g[1] + g[2] * g[2];
+      DLW(i) = dlap;
+    }
+    // AO values, gradients, laplacians; MO rows; kinetic operator B
+    for (int e = 0; e < ne; ++e) {
+      for_each_ao<double, true>(t, P(3 * e), P(3 * e + 1), P(3 * e + 2),
+                                [&](int a, const AOVal<double>& o) {
+                                  AV(e, a) = o.v;
+                                  AX(e, a) = o.gx;
+                                  AY(e, a) = o.gy;
+                                  AZ(e, a) = o.gz;
+                                  AL(e, a) = o.lap;
+                                });
+      for (int j = 0; j < nmu; ++j) {
+        double sa = 0.0, sx = 0.0, sy = 0.0, sz = 0.0, sl = 0.0;
+        for (int a = 0; a < nao; ++a) {
+          const double wv = t.W[(int64_t)a * t.ncol + j];
+          sa = fma(AV(e, a), wv, sa);
+          sx = fma(AX(e, a), wv, sx);
+          sy = fma(AY(e, a), wv, sy);
+          sz = fma(AZ(e, a), wv, sz);
+          sl = fma(AL(e, a), wv, sl);
+        }
+        MA(e, j) = sa;
+        MX(e, j) = sx;
+        MY(e, j) = sy;
+        MZ(e, j) = sz;
+        ML(e, j) = sl;
+        BK(e, j) = -0.5 * (sl + 2.0 * (GJ(e, 0) * sx + GJ(e, 1) * sy + GJ(e, 2) * sz) + LJ(e) * sa);
+        GA(e, j) = 0.0;
+        GB(e, j) = 0.0;
+      }
+    }
+    // unique spin determinants: D_u and T_u = Tr(A_u^-1 B_u)
+    const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+    MView<double> LU{sw + L.lu * ss, (int64_t)nmax * ss, ss};
+    MView<double> X{sw + L.x * ss, (int64_t)nmax * ss, ss};
+    MView<double> Y{sw + L.y * ss, (int64_t)nmax * ss, ss};
+    MView<double> Z{sw + L.z * ss, (int64_t)nmax * ss, ss};
+    double* DV = sw + L.dv * ss;
+    double* TV = sw + L.tv * ss;
+    int piv[QMC_MAX_NSPIN], cols[QMC_MAX_NSPIN];
+    auto inverse = [&](int s, int u, int n, int r0) {  // LU, X = A_u^-1; returns det
+      det_columns(d, s, u, cols);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) LU(i, j) = MA(r0 + i, cols[j]);
+      const double det = lu_factor<double>(LU, n, piv);
+      for (int i = 0; i < n; ++i)
+        for (int j = 0; j < n; ++j) X(i, j) = i == j ? 1.0 : 0.0;
+      lu_solve<double>(LU, n, piv, X.c(), X, n);
+      return det;
+    };
+    for (int s = 0; s < 2; ++s) {
+      const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0;
+      for (int u = 0; u < d.ndet[s]; ++u) {
+        double det = 1.0, tr = 0.0;
+        if (n > 0) {
+          det = inverse(s, u, n, r0);
+          for (int i = 0; i < n; ++i)
+            for (int j = 0; j < n; ++j) tr = fma(X(j, i), BK(r0 + i, cols[j]), tr);
+        }
+        const int k = (s ? d.ndet[0] : 0) + u;
+        DV[k * ss] = det;
+        TV[k * ss] = tr;
+      }
+    }
+    auto dv = [&](int s, int u) { return DV[((s ? d.ndet[0] : 0) + u) * ss]; };
+    auto tv = [&](int s, int u) { return TV[((s ? d.ndet[0] : 0) + u) * ss]; };
+    double S = 0.0, num = 0.0;
+    for (int k = 0; k < d.ncfg; ++k) {
+      const int uu = __ldg(d.cfg_det[0] + k), ud = __ldg(d.cfg_det[1] + k);
+      const double dk = dv(0, uu) * dv(1, ud), c = __ldg(d.ci_weight + k);
+      S = fma(c, dk, S);
+      num = fma(c * dk, tv(0, uu) + tv(1, ud), num);
+    }
+    const double ke = num / S;
+    for (int k = 0; k < d.ncfg; ++k) {
+      const int uu = __ldg(d.cfg_det[0] + k), ud = __ldg(d.cfg_det[1] + k);
+      const double dk = dv(0, uu) * dv(1, ud);
+      atomicAdd(&accC[k], gw * dk * (tv(0, uu) + tv(1, ud) - ke) / S);
+    }
+    // into the matrices: G_A = dKE/dA, G_B = dKE/dB (weighted by gout)
+    for (int s = 0; s < 2; ++s) {
+      const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0;
+      if (n == 0) continue;
+      for (int u = 0; u < d.ndet[s]; ++u) {
+        double dT = 0.0, dD = 0.0;
+        for (int k = 0; k < d.ncfg; ++k) {
+          if (__ldg(d.cfg_det[s] + k) != u) continue;
+          const int uo = __ldg(d.cfg_det[1 - s] + k);
+          const int uu = s ? uo : u, ud = s ? u : uo;
+          const double c = __ldg(d.ci_weight + k), dk = dv(0, uu) * dv(1, ud);
+          dT = fma(gw * c, dk / S, dT);
+          dD = fma(gw * c * (tv(0, uu) + tv(1, ud) - ke) / S, dv(1 - s, uo), dD);
+        }
+        if (dT == 0.0 && dD == 0.0) continue;
+        const double det = inverse(s, u, n, r0);
+        // Z = B_u X, Y = X Z = X B_u X
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            double z = 0.0;
+            for (int k = 0; k < n; ++k) z = fma(BK(r0 + i, cols[k]), X(k, j), z);
+            Z(i, j) = z;
+          }
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            double y = 0.0;
+            for (int k = 0; k < n; ++k) y = fma(X(i, k), Z(k, j), y);
+            Y(i, j) = y;
+          }
+        const double sd = dD * det;
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) {
+            GA(r0 + i, cols[j]) += sd * X(j, i) - dT * Y(j, i);
+            GB(r0 + i, cols[j]) += dT * X(j, i);
+          }
+      }
+    }
+    // through B: dA_total = G_A - lapJ/2 G_B, d lapMO = -G_B/2, d gradMO = -gradU G_B;
+    // Jastrow weight through grad U and lap U + |grad U|^2
+    double dwj = 0.0;
+    for (int e = 0; e < ne; ++e) {
+      double dg[3] = {0.0, 0.0, 0.0}, dl = 0.0;
+      for (int j = 0; j < nmu; ++j) {
+        const double gb = GB(e, j);
+        dg[0] -= gb * MX(e, j);
+        dg[1] -= gb * MY(e, j);
+        dg[2] -= gb * MZ(e, j);
+        dl -= 0.5 * gb * MA(e, j);
+        GA(e, j) -= 0.5 * LJ(e) * gb;
+      }
+      if (d.use_jastrow) {
+        double gdg = 0.0;
+        for (int x = 0; x < 3; ++x) {
+          dwj = fma(dg[x], DGW(e, x), dwj);
+          gdg = fma(GJ(e, x), DGW(e, x), gdg);
+        }
+        dwj = fma(dl, DLW(e) + 2.0 * gdg, dwj);
+      }
+    }
+    if (d.use_jastrow) atomicAdd(accJ, dwj);
+    // W[a][j]: sum_e AO(e,a) dA(e,j) - (lap AO(e,a) / 2 + gradU(e) . grad AO(e,a)) G_B(e,j)
+    for (int a = 0; a < nao; ++a)
+      for (int j = 0; j < nmu; ++j) {
+        double sum = 0.0;
+        for (int e = 0; e < ne; ++e) {
+          const double hb = 0.5 * AL(e, a) + GJ(e, 0) * AX(e, a) + GJ(e, 1) * AY(e, a) +
+                            GJ(e, 2) * AZ(e, a);
+          sum = fma(AV(e, a), GA(e, j), sum);
+          sum = fma(-hb, GB(e, j), sum);
+        }
+        if (sum != 0.0) atomicAdd(&accW[a * nmu + j], sum);
+      }
+    // exponents: hA = sum_j dA W, hB = sum_j G_B W per AO; per primitive p
+    //   d val / d alpha  = -vs w_p P r^2 e_p
+    //   d grad / d alpha = w_p e_p (-r^2 dP - 2 r P (1 - alpha r^2))
+    //   d lap / d alpha  = vs w_p e_p (-r^2 lapP + P (8 r^2 alpha - 4 r^4 alpha^2
+    //                      - (6 + 4 l)(1 - alpha r^2)))
+    for (int e = 0; e < ne; ++e) {
+      const double ex = P(3 * e), ey = P(3 * e + 1), ez = P(3 * e + 2);
+      const double gx = GJ(e, 0), gy = GJ(e, 1), gz = GJ(e, 2);
+      for (int g = 0; g < t.ngroup; ++g) {
+        const int A = t.group_atom[g];
+        const double dx = ex - t.atom_xyz[3 * A], dy = ey - t.atom_xyz[3 * A + 1],
+                     dz = ez - t.atom_xyz[3 * A + 2];
+        const double r2 = dx * dx + dy * dy + dz * dz;
+        const int np = t.group_prim[g + 1] - t.group_prim[g];
+        for (int a = t.group_ao[g]; a < t.group_ao[g + 1]; ++a) {
+          double ha = 0.0, hb = 0.0;
+          for (int j = 0; j < nmu; ++j) {
+            const double wv = t.W[(int64_t)a * t.ncol + j];
+            ha = fma(GA(e, j), wv, ha);
+            hb = fma(GB(e, j), wv, hb);
+          }
+          if (ha == 0.0 && hb == 0.0) continue;
+          const int kx = t.ao_k[3 * a], ky = t.ao_k[3 * a + 1], kz = t.ao_k[3 * a + 2];
+          const Poly<double> pl = cart_poly<double, true>(dx, dy, dz, kx, ky, kz);
+          const int l = kx + ky + kz;
+          const double vs = t.vscale ? t.vscale[a] : 1.0;
+          for (int p = 0; p < np; ++p) {
+            const int wi = t.ao_wofs[a] + p;
+            const double al = t.walpha[wi], wp = t.wd[wi], ep = exp(-al * r2);
+            const double q = 1.0 - al * r2;
+            const double dval = -vs * wp * pl.p * r2 * ep;
+            const double dgx = wp * ep * (-r2 * pl.dx - 2.0 * dx * pl.p * q);
+            const double dgy = wp * ep * (-r2 * pl.dy - 2.0 * dy * pl.p * q);
+            const double dgz = wp * ep * (-r2 * pl.dz - 2.0 * dz * pl.p * q);
+            const double dlap = vs * wp * ep *
+                                (-r2 * pl.lap + pl.p * (8.0 * r2 * al - 4.0 * r2 * r2 * al * al -
+                                                        (double)(6 + 4 * l) * q));
+            const double c = ha * dval - hb * (0.5 * dlap + gx * dgx + gy * dgy + gz * dgz);
+            atomicAdd(&accE[__ldg(w_entry + wi)], c);
+          }
+        }
+      }
+    }
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < nao * nmu; i += blockDim.x) {
+    const int a = i / nmu, j = i - a * nmu;
+    if (accW[i] != 0.0) atomicAdd(&g_W[(int64_t)a * ldw + j], accW[i]);
+  }
+  for (int i = threadIdx.x; i < nent; i += blockDim.x)
+    if (accE[i] != 0.0) atomicAdd(&g_exp[i], accE[i]);
+  for (int i = threadIdx.x; i < d.ncfg; i += blockDim.x) atomicAdd(&g_ci[i], accC[i]);
+  if (threadIdx.x == 0 && g_jw) atomicAdd(g_jw, accJ[0]);
+}
+
 }  // namespace qmc
 
 using namespace qmc;
@@ -244,6 +576,37 @@ int qmc_wf_psi_adjoint(const qmc_wf_desc* d0, const double* pos, int64_t nw, con
   if ((st = prepare_smem(psi_adjoint_kernel, smem))) return st;
   const dim3 grid((unsigned)((nw + kAdjTPB - 1) / kAdjTPB));
   psi_adjoint_kernel<<<grid, kAdjTPB, smem, (cudaStream_t)stream>>>(
+      dd, pos, nw, gout, weight_entry, nentries, grad_exp, grad_W, ldw,
+      d->use_jastrow ? grad_jastrow_w : nullptr, grad_ci, (double*)scratch, pad_walkers(nw));
+  return launch_status();
+}
+
+int64_t qmc_eloc_adjoint_scratch_bytes(const qmc_wf_desc* d, int64_t nw) {
+  if (check_desc(d) != QMC_OK || nw < 0) return -1;
+  return el_adj_layout(*d).total * pad_walkers(nw) * (int64_t)sizeof(double);
+}
+
+int qmc_wf_local_energy_adjoint(const qmc_wf_desc* d0, const double* pos, int64_t nw,
+                                const double* gout, const int32_t* weight_entry, int32_t nentries,
+                                double* grad_exp, double* grad_W, int32_t ldw,
+                                double* grad_jastrow_w, double* grad_ci, void* scratch,
+                                int64_t scratch_bytes, void* stream) {
+  int st = check_desc(d0);
+  if (st) return st;
+  qmc_wf_desc dd = *d0;
+  dd.precision = QMC_PREC_FP64;  // the adjoint is FP64
+  const qmc_wf_desc* d = &dd;
+  if (nw < 0 || nentries < 0 || ldw < d->nmo_used) return QMC_ERR_ARG;
+  if (nw > 0 && (!pos || !gout || !weight_entry || !grad_exp || !grad_W || !grad_ci || !scratch))
+    return QMC_ERR_ARG;
+  if (nw == 0) return QMC_OK;
+  if (scratch_bytes < qmc_eloc_adjoint_scratch_bytes(d, nw)) return QMC_ERR_SCRATCH;
+  const int ncol = round_up(d->nmo_used, 8);
+  const int64_t smem = ((tables_smem_bytes<double>(*d, ncol) + 15) & ~int64_t(15)) +
+                       adj_acc_doubles(*d, nentries) * 8;
+  if ((st = prepare_smem(eloc_adjoint_kernel, smem))) return st;
+  const dim3 grid((unsigned)((nw + kAdjTPB - 1) / kAdjTPB));
+  eloc_adjoint_kernel<<<grid, kAdjTPB, smem, (cudaStream_t)stream>>>(
       dd, pos, nw, gout, weight_entry, nentries, grad_exp, grad_W, ldw,
       d->use_jastrow ? grad_jastrow_w : nullptr, grad_ci, (double*)scratch, pad_walkers(nw));
   return launch_status();

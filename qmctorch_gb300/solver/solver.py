@@ -274,11 +274,11 @@ class Solver(SolverBase):
         return cumulative_loss
 
     def evaluate_grad_auto(self, lpos):
-        """solver.py:352-370: gradient of the loss through the local energy.
-        The local-energy kernel has no adjoint here; use grad="manual" (the
-        reference's default), whose psi adjoint is hand-written."""
-        raise NotImplementedError("grad='auto' (differentiating the local energy) is not on the "
-                                  "GB300 path; use grad='manual'")
+        """solver.py:352-370: gradient of the loss through the local energy
+        (hand-written local-energy adjoint behind wf.local_energy)."""
+        loss, eloc = self.loss(lpos)
+        loss.backward()
+        return loss, eloc
 
     def evaluate_grad_manual(self, lpos):
         """solver.py:372-431: dE/dk = 2 < (E_L - <E_L>) dpsi/dk / psi >."""

@@ -91,6 +91,30 @@ class _PsiFunction(torch.autograd.Function):
                 g_w if need[3] else None, g_fc if need[4] else None, None)
 
 
+class _ElocFunction(torch.autograd.Function):
+    """Local energy with a hand-written adjoint (``qmc_wf_local_energy_adjoint``)
+    for the trainable parameters, positions held fixed; AO values and
+    derivatives are recomputed in the backward pass."""
+
+    @staticmethod
+    def forward(ctx, x, bas_exp, mo_modifier, jastrow_w, fc_weight, wf):
+        ctx.wf = wf
+        xd = rt.dev64(x, rt.cuda_device()).reshape(-1, wf.ndim_tot)
+        ctx.save_for_backward(xd)
+        el, _ = wf._eloc(xd)
+        return el.reshape(-1, 1).to(device=x.device, dtype=x.dtype)
+
+    @staticmethod
+    def backward(ctx, gout):
+        (xd,) = ctx.saved_tensors
+        wf = ctx.wf
+        g_exp, g_mod, g_w, g_fc = wf._adjoint(xd, gout.reshape(-1), "qmc_wf_local_energy_adjoint",
+                                              "qmc_eloc_adjoint_scratch_bytes")
+        need = ctx.needs_input_grad
+        return (None, g_exp if need[1] else None, g_mod if need[2] else None,
+                g_w if need[3] else None, g_fc if need[4] else None, None)
+
+
 class SlaterJastrow(WaveFunction):
     """``precision`` (keyword added to the reference signature) selects the
     arithmetic of the fused psi / local-energy / Metropolis kernels: "fp64"
@@ -225,6 +249,11 @@ class SlaterJastrow(WaveFunction):
 
     def _psi_adjoint(self, x, gout):
         """Parameter gradients of sum_w gout[w] psi_w (qmc_wf_psi_adjoint)."""
+        return self._adjoint(x, gout, "qmc_wf_psi_adjoint", "qmc_adjoint_scratch_bytes")
+
+    def _adjoint(self, x, gout, fn, scratch_fn):
+        """Parameter gradients of sum_w gout[w] f_w by the adjoint entry point
+        ``fn`` (psi or the local energy)."""
         device = rt.cuda_device()
         nb = x.shape[0]
         call = self._desc(device)
@@ -236,11 +265,11 @@ class SlaterJastrow(WaveFunction):
         g_W = torch.zeros((self.ao.norb, nmu), dtype=rt.F64, device=device)
         g_w = torch.zeros(1, dtype=rt.F64, device=device)
         g_ci = torch.zeros(self.nci, dtype=rt.F64, device=device)
-        scr = rt.scratch(lib.qmc_adjoint_scratch_bytes(call.ref, nb), device)
-        _lib.check(lib.qmc_wf_psi_adjoint(call.ref, rt.ptr(x), nb, rt.ptr(g), rt.ptr(bt.t["w_entry"]),
-                                          bt.nentries, rt.ptr(g_exp), rt.ptr(g_W), nmu,
-                                          rt.ptr(g_w), rt.ptr(g_ci), rt.ptr(scr), scr.numel(),
-                                          rt.stream_handle()), "qmc_wf_psi_adjoint")
+        scr = rt.scratch(getattr(lib, scratch_fn)(call.ref, nb), device)
+        _lib.check(getattr(lib, fn)(call.ref, rt.ptr(x), nb, rt.ptr(g), rt.ptr(bt.t["w_entry"]),
+                                    bt.nentries, rt.ptr(g_exp), rt.ptr(g_W), nmu, rt.ptr(g_w),
+                                    rt.ptr(g_ci), rt.ptr(scr), scr.numel(), rt.stream_handle()),
+                   fn)
         mod = self.mo.mo_modifier
         g_mod = torch.zeros(mod.shape, dtype=rt.F64, device=device)
         g_mod[:, :nmu] = g_W * rt.dev64(self.mo.mo_scf, device)[:, :nmu]
@@ -257,7 +286,13 @@ class SlaterJastrow(WaveFunction):
         return (psi * psi).to(device=pos.device, dtype=pos.dtype)
 
     def local_energy(self, pos):
-        """E_L = KE + V_en + V_ee + V_nn -> (nbatch, 1) (wf_base.py:184-215)."""
+        """E_L = KE + V_en + V_ee + V_nn -> (nbatch, 1) (wf_base.py:184-215).
+        Differentiable with respect to ao.bas_exp, mo.mo_modifier,
+        jastrow.jastrow_kernel.weight and fc.weight (hand-written adjoint)."""
+        jw = self.jastrow.jastrow_kernel.weight if self.use_jastrow else self._no_jastrow_w
+        params = (self.ao.bas_exp, self.mo.mo_modifier, jw, self.fc.weight)
+        if torch.is_grad_enabled() and any(p.requires_grad for p in params):
+            return _ElocFunction.apply(pos, *params, self)
         el, _ = self._eloc(pos)
         return el.reshape(-1, 1).to(device=pos.device, dtype=pos.dtype)
 
