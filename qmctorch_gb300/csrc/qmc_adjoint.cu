@@ -2,8 +2,10 @@
 // (ao.bas_exp, mo.mo_modifier through W = mo_scf * mo_modifier,
 // jastrow.jastrow_kernel.weight, fc.weight), FP64, one thread per walker.
 // The AO values are recomputed from the positions, not stored by the forward
-// pass. Walker contributions, weighted by gout[w], are summed in shared
-// memory and added to the outputs with one global atomic per block.
+// pass. Each walker writes its contributions, weighted by gout[w], to its own
+// slots of the scratch; adj_reduce_kernel then sums every parameter over the
+// walkers in a fixed order, so the gradients are bitwise reproducible and
+// independent of the launch configuration (no atomics).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -40,8 +42,14 @@ __device__ inline void det_columns(const qmc_wf_desc& d, int spin, int u, int* c
 }
 
 struct AdjLayout {  // per-walker scratch, in doubles (item-major)
-  int64_t ao, mo, g, lu, inv, dv, total;
+  int64_t ao, mo, g, lu, inv, dv, gacc, total;
 };
+
+// Per-walker gradient slots: W [nao][nmu], exponents [nweight] (one per basis
+// entry), CI weights [ncfg], Pade weight [1].
+__host__ __device__ inline int64_t adj_acc_doubles(const qmc_wf_desc& d) {
+  return (int64_t)d.nao * d.nmo_used + d.nweight + d.ncfg + 1;
+}
 
 __host__ __device__ inline AdjLayout adj_layout(const qmc_wf_desc& d) {
   AdjLayout L;
@@ -59,36 +67,30 @@ __host__ __device__ inline AdjLayout adj_layout(const qmc_wf_desc& d) {
   o += nmax * nmax;
   L.dv = o;
   o += d.ndet[0] + d.ndet[1];
+  L.gacc = o;
+  o += adj_acc_doubles(d);
   L.total = o;
   return L;
 }
 
-__host__ __device__ inline int64_t adj_acc_doubles(const qmc_wf_desc& d, int nent) {
-  return (int64_t)d.nao * d.nmo_used + nent + d.ncfg + 1;
-}
-
 __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
     const qmc_wf_desc d, const double* __restrict__ pos, int64_t nw, const double* __restrict__ gout,
-    const int* __restrict__ w_entry, int nent, double* __restrict__ g_exp,
-    double* __restrict__ g_W, int ldw, double* __restrict__ g_jw, double* __restrict__ g_ci,
-    double* __restrict__ scr, int64_t ss) {
+    const int* __restrict__ w_entry, double* __restrict__ scr, int64_t ss) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int ncol = round_up(d.nmo_used, 8);
   const Tables<double> t = load_tables<double>(d, d.nmo_used, ncol, smem);
-  double* acc = reinterpret_cast<double*>(smem + ((tables_smem_bytes<double>(d, ncol) + 15) & ~15));
   const int nmu = d.nmo_used, ne = d.nelec, nao = d.nao;
-  double* accW = acc;                    // [nao][nmu]
-  double* accE = accW + nao * nmu;       // [nent]
-  double* accC = accE + nent;            // [ncfg]
-  double* accJ = accC + d.ncfg;          // [1]
-  const int64_t nacc = adj_acc_doubles(d, nent);
-  for (int64_t i = threadIdx.x; i < nacc; i += blockDim.x) acc[i] = 0.0;
-  __syncthreads();
   const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (w < nw) {
     const double gw = gout[w];
     const AdjLayout L = adj_layout(d);
     double* sw = scr + w;
+    // this walker's gradient slots
+    double* const accW = sw + L.gacc * ss;  // [nao * nmu] (stride ss)
+    double* const accE = accW + (int64_t)nao * nmu * ss;
+    double* const accC = accE + (int64_t)d.nweight * ss;
+    double* const accJ = accC + (int64_t)d.ncfg * ss;
+    for (int64_t i = 0; i < adj_acc_doubles(d); ++i) accW[i * ss] = 0.0;
     auto AO = [&](int e, int a) -> double& { return sw[(L.ao + (int64_t)e * nao + a) * ss]; };
     auto MO = [&](int e, int j) -> double& { return sw[(L.mo + (int64_t)e * nmu + j) * ss]; };
     auto G = [&](int e, int j) -> double& { return sw[(L.g + (int64_t)e * nmu + j) * ss]; };
@@ -144,9 +146,9 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
     for (int k = 0; k < d.ncfg; ++k) {
       const double dd = dval(0, __ldg(d.cfg_det[0] + k)) * dval(1, __ldg(d.cfg_det[1] + k));
       psid = fma(__ldg(d.ci_weight + k), dd, psid);
-      atomicAdd(&accC[k], gw * J * dd);  // d psi / d c_k
+      accC[k * ss] += gw * J * dd;  // d psi / d c_k
     }
-    if (d.use_jastrow) atomicAdd(accJ, gw * J * psid * dlogj);  // d psi / d w
+    if (d.use_jastrow) accJ[0] += gw * J * psid * dlogj;  // d psi / d w
     // d psi / d MO = J sum_u coef_u det_u A_u^-T (scattered into the columns of u)
     for (int s = 0; s < 2; ++s) {
       const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0;
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
       for (int j = 0; j < nmu; ++j) {
         double s = 0.0;
         for (int e = 0; e < ne; ++e) s = fma(AO(e, a), G(e, j), s);
-        if (s != 0.0) atomicAdd(&accW[a * nmu + j], gw * s);
+        accW[((int64_t)a * nmu + j) * ss] = gw * s;
       }
     // d psi / d alpha_p = sum_e H[e][a] dAO[e][a]/d alpha_p, H = G W^T,
     // dAO/d alpha_p = -vs w_p P r^2 exp(-alpha_p r^2) (the norm is a constant)
@@ -196,21 +198,12 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
           for (int p = 0; p < np; ++p) {
             const int wi = t.ao_wofs[a] + p;
             const double dao = -vs * t.wd[wi] * pl.p * r2 * exp(-t.walpha[wi] * r2);
-            atomicAdd(&accE[__ldg(w_entry + wi)], gw * h * dao);
+            accE[(int64_t)__ldg(w_entry + wi) * ss] += gw * h * dao;
           }
         }
       }
     }
   }
-  __syncthreads();
-  for (int i = threadIdx.x; i < nao * nmu; i += blockDim.x) {
-    const int a = i / nmu, j = i - a * nmu;
-    if (accW[i] != 0.0) atomicAdd(&g_W[(int64_t)a * ldw + j], accW[i]);
-  }
-  for (int i = threadIdx.x; i < nent; i += blockDim.x)
-    if (accE[i] != 0.0) atomicAdd(&g_exp[i], accE[i]);
-  for (int i = threadIdx.x; i < d.ncfg; i += blockDim.x) atomicAdd(&g_ci[i], accC[i]);
-  if (threadIdx.x == 0 && g_jw) atomicAdd(g_jw, accJ[0]);
 }
 
 
@@ -228,7 +221,7 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
 // norms fixed) to the exponents, and through grad U, lap U to the Pade weight.
 struct ElAdjLayout {  // per-walker scratch, in doubles (item-major)
   int64_t aov, aox, aoy, aoz, aol, ma, mx, my, mz, ml, b, ga, gb, lu, x, y, z, dv, tv, gj, lj,
-      dgw, dlw, total;
+      dgw, dlw, gacc, total;
 };
 
 __host__ __device__ inline ElAdjLayout el_adj_layout(const qmc_wf_desc& d) {
@@ -264,32 +257,29 @@ __host__ __device__ inline ElAdjLayout el_adj_layout(const qmc_wf_desc& d) {
   L.lj = take(ne);
   L.dgw = take(3 * ne);
   L.dlw = take(ne);
+  L.gacc = take(adj_acc_doubles(d));
   L.total = o;
   return L;
 }
 
 __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
     const qmc_wf_desc d, const double* __restrict__ pos, int64_t nw, const double* __restrict__ gout,
-    const int* __restrict__ w_entry, int nent, double* __restrict__ g_exp,
-    double* __restrict__ g_W, int ldw, double* __restrict__ g_jw, double* __restrict__ g_ci,
-    double* __restrict__ scr, int64_t ss) {
+    const int* __restrict__ w_entry, double* __restrict__ scr, int64_t ss) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int ncol = round_up(d.nmo_used, 8);
   const Tables<double> t = load_tables<double>(d, d.nmo_used, ncol, smem);
-  double* acc = reinterpret_cast<double*>(smem + ((tables_smem_bytes<double>(d, ncol) + 15) & ~15));
   const int nmu = d.nmo_used, ne = d.nelec, nao = d.nao;
-  double* accW = acc;               // [nao][nmu]
-  double* accE = accW + nao * nmu;  // [nent]
-  double* accC = accE + nent;       // [ncfg]
-  double* accJ = accC + d.ncfg;     // [1]
-  const int64_t nacc = adj_acc_doubles(d, nent);
-  for (int64_t i = threadIdx.x; i < nacc; i += blockDim.x) acc[i] = 0.0;
-  __syncthreads();
   const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (w < nw) {
     const double gw = gout[w];
     const ElAdjLayout L = el_adj_layout(d);
     double* sw = scr + w;
+    // this walker's gradient slots
+    double* const accW = sw + L.gacc * ss;  // [nao * nmu] (stride ss)
+    double* const accE = accW + (int64_t)nao * nmu * ss;
+    double* const accC = accE + (int64_t)d.nweight * ss;
+    double* const accJ = accC + (int64_t)d.ncfg * ss;
+    for (int64_t i = 0; i < adj_acc_doubles(d); ++i) accW[i * ss] = 0.0;
     auto R2 = [&](int64_t base, int e, int k, int n) -> double& {
       return sw[(base + (int64_t)e * n + k) * ss];
     };
@@ -416,7 +406,7 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
     for (int k = 0; k < d.ncfg; ++k) {
       const int uu = __ldg(d.cfg_det[0] + k), ud = __ldg(d.cfg_det[1] + k);
       const double dk = dv(0, uu) * dv(1, ud);
-      atomicAdd(&accC[k], gw * dk * (tv(0, uu) + tv(1, ud) - ke) / S);
+      accC[k * ss] += gw * dk * (tv(0, uu) + tv(1, ud) - ke) / S;
     }
     // into the matrices: G_A = dKE/dA, G_B = dKE/dB (weighted by gout)
     for (int s = 0; s < 2; ++s) {
@@ -477,7 +467,7 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
         dwj = fma(dl, DLW(e) + 2.0 * gdg, dwj);
       }
     }
-    if (d.use_jastrow) atomicAdd(accJ, dwj);
+    if (d.use_jastrow) accJ[0] += dwj;
     // W[a][j]: sum_e AO(e,a) dA(e,j) - (lap AO(e,a) / 2 + gradU(e) . grad AO(e,a)) G_B(e,j)
     for (int a = 0; a < nao; ++a)
       for (int j = 0; j < nmu; ++j) {
@@ -488,7 +478,7 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
           sum = fma(AV(e, a), GA(e, j), sum);
           sum = fma(-hb, GB(e, j), sum);
         }
-        if (sum != 0.0) atomicAdd(&accW[a * nmu + j], sum);
+        accW[((int64_t)a * nmu + j) * ss] = sum;
       }
     // exponents: hA = sum_j dA W, hB = sum_j G_B W per AO; per primitive p
     //   d val / d alpha  = -vs w_p P r^2 e_p
@@ -528,21 +518,46 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
                                 (-r2 * pl.lap + pl.p * (8.0 * r2 * al - 4.0 * r2 * r2 * al * al -
                                                         (double)(6 + 4 * l) * q));
             const double c = ha * dval - hb * (0.5 * dlap + gx * dgx + gy * dgy + gz * dgz);
-            atomicAdd(&accE[__ldg(w_entry + wi)], c);
+            accE[(int64_t)__ldg(w_entry + wi) * ss] += c;
           }
         }
       }
     }
   }
+}
+
+// Sum of parameter i's walker slots in a fixed order (per-thread strided
+// partial sums, then a fixed tree), added to its output: W (row stride ldw),
+// exponents, CI weights, Pade weight. One block per parameter.
+constexpr int kRedTPB = 256;
+__global__ void __launch_bounds__(kRedTPB) adj_reduce_kernel(
+    const double* __restrict__ gacc, int64_t nw, int64_t ss, int nao, int nmu, int nweight,
+    int nent, int ncfg, double* __restrict__ g_W, int ldw, double* __restrict__ g_exp,
+    double* __restrict__ g_ci, double* __restrict__ g_jw) {
+  __shared__ double sh[kRedTPB];
+  const int64_t i = blockIdx.x;
+  const double* row = gacc + i * ss;
+  double s = 0.0;
+  for (int64_t w = threadIdx.x; w < nw; w += kRedTPB) s += row[w];
+  sh[threadIdx.x] = s;
   __syncthreads();
-  for (int i = threadIdx.x; i < nao * nmu; i += blockDim.x) {
-    const int a = i / nmu, j = i - a * nmu;
-    if (accW[i] != 0.0) atomicAdd(&g_W[(int64_t)a * ldw + j], accW[i]);
+  for (int h = kRedTPB / 2; h > 0; h >>= 1) {
+    if (threadIdx.x < h) sh[threadIdx.x] += sh[threadIdx.x + h];
+    __syncthreads();
   }
-  for (int i = threadIdx.x; i < nent; i += blockDim.x)
-    if (accE[i] != 0.0) atomicAdd(&g_exp[i], accE[i]);
-  for (int i = threadIdx.x; i < d.ncfg; i += blockDim.x) atomicAdd(&g_ci[i], accC[i]);
-  if (threadIdx.x == 0 && g_jw) atomicAdd(g_jw, accJ[0]);
+  if (threadIdx.x != 0) return;
+  const double v = sh[0];
+  const int64_t nw_ = (int64_t)nao * nmu;
+  if (i < nw_) {
+    g_W[(i / nmu) * ldw + i % nmu] += v;
+  } else if (i < nw_ + nweight) {
+    const int e = (int)(i - nw_);
+    if (e < nent) g_exp[e] += v;
+  } else if (i < nw_ + nweight + ncfg) {
+    g_ci[i - nw_ - nweight] += v;
+  } else if (g_jw) {
+    g_jw[0] += v;
+  }
 }
 
 }  // namespace qmc
@@ -570,14 +585,18 @@ int qmc_wf_psi_adjoint(const qmc_wf_desc* d0, const double* pos, int64_t nw, con
     return QMC_ERR_ARG;
   if (nw == 0) return QMC_OK;
   if (scratch_bytes < qmc_adjoint_scratch_bytes(d, nw)) return QMC_ERR_SCRATCH;
+  if (nentries > d->nweight) return QMC_ERR_ARG;
   const int ncol = round_up(d->nmo_used, 8);
-  const int64_t smem = ((tables_smem_bytes<double>(*d, ncol) + 15) & ~int64_t(15)) +
-                       adj_acc_doubles(*d, nentries) * 8;
+  const int64_t smem = tables_smem_bytes<double>(*d, ncol);
   if ((st = prepare_smem(psi_adjoint_kernel, smem))) return st;
   const dim3 grid((unsigned)((nw + kAdjTPB - 1) / kAdjTPB));
-  psi_adjoint_kernel<<<grid, kAdjTPB, smem, (cudaStream_t)stream>>>(
-      dd, pos, nw, gout, weight_entry, nentries, grad_exp, grad_W, ldw,
-      d->use_jastrow ? grad_jastrow_w : nullptr, grad_ci, (double*)scratch, pad_walkers(nw));
+  const int64_t ss = pad_walkers(nw);
+  cudaStream_t cs = (cudaStream_t)stream;
+  psi_adjoint_kernel<<<grid, kAdjTPB, smem, cs>>>(dd, pos, nw, gout, weight_entry, (double*)scratch, ss);
+  const double* gacc = (const double*)scratch + adj_layout(dd).gacc * ss;
+  adj_reduce_kernel<<<(unsigned)adj_acc_doubles(dd), kRedTPB, 0, cs>>>(
+      gacc, nw, ss, dd.nao, dd.nmo_used, dd.nweight, nentries, dd.ncfg, grad_W, ldw, grad_exp,
+      grad_ci, d->use_jastrow ? grad_jastrow_w : nullptr);
   return launch_status();
 }
 
@@ -601,14 +620,18 @@ int qmc_wf_local_energy_adjoint(const qmc_wf_desc* d0, const double* pos, int64_
     return QMC_ERR_ARG;
   if (nw == 0) return QMC_OK;
   if (scratch_bytes < qmc_eloc_adjoint_scratch_bytes(d, nw)) return QMC_ERR_SCRATCH;
+  if (nentries > d->nweight) return QMC_ERR_ARG;
   const int ncol = round_up(d->nmo_used, 8);
-  const int64_t smem = ((tables_smem_bytes<double>(*d, ncol) + 15) & ~int64_t(15)) +
-                       adj_acc_doubles(*d, nentries) * 8;
+  const int64_t smem = tables_smem_bytes<double>(*d, ncol);
   if ((st = prepare_smem(eloc_adjoint_kernel, smem))) return st;
   const dim3 grid((unsigned)((nw + kAdjTPB - 1) / kAdjTPB));
-  eloc_adjoint_kernel<<<grid, kAdjTPB, smem, (cudaStream_t)stream>>>(
-      dd, pos, nw, gout, weight_entry, nentries, grad_exp, grad_W, ldw,
-      d->use_jastrow ? grad_jastrow_w : nullptr, grad_ci, (double*)scratch, pad_walkers(nw));
+  const int64_t ss = pad_walkers(nw);
+  cudaStream_t cs = (cudaStream_t)stream;
+  eloc_adjoint_kernel<<<grid, kAdjTPB, smem, cs>>>(dd, pos, nw, gout, weight_entry, (double*)scratch, ss);
+  const double* gacc = (const double*)scratch + el_adj_layout(dd).gacc * ss;
+  adj_reduce_kernel<<<(unsigned)adj_acc_doubles(dd), kRedTPB, 0, cs>>>(
+      gacc, nw, ss, dd.nao, dd.nmo_used, dd.nweight, nentries, dd.ncfg, grad_W, ldw, grad_exp,
+      grad_ci, d->use_jastrow ? grad_jastrow_w : nullptr);
   return launch_status();
 }
 

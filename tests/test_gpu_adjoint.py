@@ -158,3 +158,25 @@ def test_local_energy_adjoint_against_finite_differences(name):
                 fd = (fp - fm) / (2 * h)
                 ad = float(p.grad.view(-1)[i])
                 assert abs(fd - ad) <= 1e-5 * max(1.0, abs(fd)), (n, i, fd, ad)
+
+
+def test_gradients_are_bitwise_reproducible():
+    """The adjoints sum walker contributions in a fixed order (no atomics):
+    repeated backward passes give identical bits, for psi and for E_L."""
+    mol, d = load("h2o_sd")
+    wf = make_wf(mol, d)
+    rng = np.random.default_rng(8)
+    centers = np.repeat(np.asarray(mol.atom_coords), mol.atomic_nelec, axis=0)
+    pos = torch.as_tensor((centers[None] + rng.normal(size=(3000, 10, 3))).reshape(3000, -1),
+                          device="cuda")
+    g = torch.as_tensor(rng.normal(size=3000), device="cuda")
+    params = dict(wf.named_parameters())
+    for f in (lambda: wf(pos), lambda: wf.local_energy(pos)):
+        grads = []
+        for _ in range(2):
+            for p in params.values():
+                p.grad = None
+            (f().reshape(-1) * g).sum().backward()
+            grads.append([params[n].grad.detach().clone() for n in PARAMS])
+        for a, b in zip(*grads):
+            assert torch.equal(a, b)
