@@ -242,9 +242,9 @@ def precision_study(torch, wf64, wfm, x_eq, sampler, nfixed=100_000):
         snaps.append(x.clone())
         n += x.shape[0]
     X = torch.cat(snaps)[:nfixed]
-    e64 = wf64.local_energy(X).reshape(-1).double()
-    em = wfm.local_energy(X).reshape(-1).double()
     with torch.no_grad():
+        e64 = wf64.local_energy(X).reshape(-1).double()
+        em = wfm.local_energy(X).reshape(-1).double()
         p64 = wf64(X).reshape(-1).double()
         pm = wfm(X).reshape(-1).double()
     de = (em - e64).abs()

@@ -1,12 +1,19 @@
-"""Continuous-batching VMC single-point server on one GPU.
+"""Continuous-batching VMC server on one GPU: single-point and VMC-run jobs.
 
-The reference has no serving layer; its unit of work is
-``Solver.single_point()`` (solver_base.py:316-387): sample the wave function
+The reference has no serving layer; its units of work are
+``Solver.single_point()`` (solver_base.py:316-387: sample the wave function
 with Metropolis, evaluate the local energy on the kept walkers, report mean,
-variance and sampling error. A request here is one such single point
-(``nstep`` all-electron Metropolis steps from seeded positions, the last
-positions kept as with the sampler's default ``ntherm = -1``), for any
-molecule the kernels support.
+variance and sampling error) and ``Solver.run()`` (solver.py:186-350: energy
+minimisation with the manual gradient, an optimizer step per epoch and
+``nstep_update`` resampling steps after it). A request is one of these:
+
+* ``kind="single_point"``: ``nstep`` all-electron Metropolis steps from
+  seeded positions (the last positions kept, as with the sampler's default
+  ``ntherm = -1``), then the local energy and its statistics;
+* ``kind="run"``: the same initial sampling, then ``nepoch`` epochs of
+  (manual gradient 2 <(E_L - <E_L>) dpsi / psi> through the hand-written psi
+  adjoint, Adam step, ``nstep_update`` resampling steps), then the final
+  single point; the result also holds the mean local energy of every epoch.
 
 Scheduling (``Scheduler``):
 
@@ -59,6 +66,10 @@ class Request:
     step_size: float = 0.2
     seed: int = 0
     precision: str = "mixed"
+    kind: str = "single_point"   # or "run"
+    nepoch: int = 0              # run: optimisation epochs
+    lr: float = 1e-3             # run: Adam learning rate
+    nstep_update: int = 25       # run: resampling steps after each epoch
     rid: int = -1
     arrival: float = 0.0
 
@@ -74,6 +85,7 @@ class Result:
     arrival: float
     admitted: float
     done: float
+    energies: list = None  # run: mean local energy of each epoch
 
     @property
     def latency(self):
@@ -87,10 +99,12 @@ class _Job:
     footprint: int
     admitted: float
     steps_done: int = 0
-    inflight: object = None      # token of the slice or energy work in flight
-    phase: str = "sampling"      # sampling -> energy -> (retired)
+    inflight: object = None      # token of the slice, gradient or energy work in flight
+    phase: str = "sampling"      # sampling [-> grad -> sampling]* -> energy -> (retired)
     handle: object = None        # executor state
     order: int = 0
+    target: int = 0              # Metropolis steps to reach before the next phase
+    epoch: int = 0               # run: epochs done
 
 
 class Scheduler:
@@ -117,6 +131,8 @@ class Scheduler:
 
     # -- public API -------------------------------------------------------
     def submit(self, req):
+        if req.kind not in ("single_point", "run"):
+            raise ValueError("request kind must be 'single_point' or 'run'")
         req.rid = self.next_rid
         self.next_rid += 1
         req.arrival = self.clock()
@@ -160,21 +176,29 @@ class Scheduler:
             if job.inflight is not None and self.ex.ready(job.inflight):
                 job.inflight = None
                 if job.phase == "energy":
-                    e, v, err = self.ex.stats(job.handle)
+                    e, v, err, energies = self.ex.stats(job.handle)
                     r = Result(job.req.rid, e, v, err, job.req.nwalkers, job.req.nstep,
-                               job.req.arrival, job.admitted, self.clock())
+                               job.req.arrival, job.admitted, self.clock(), energies)
                     self.results[r.rid] = r
                     out.append(r)
                     self.ex.release(job.handle)
                     self.used -= job.footprint
                     continue
+                if job.phase == "grad":  # epoch done: resample
+                    job.epoch += 1
+                    job.target += job.req.nstep_update
+                    job.phase = "sampling"
             keep.append(job)
         self.active = keep
-        # jobs whose sampling finished go to the energy phase
+        # jobs whose sampling reached its target: next epoch or the final energy
         for job in self.active:
-            if job.phase == "sampling" and job.inflight is None and job.steps_done >= job.req.nstep:
-                job.phase = "energy"
-                job.inflight = self.ex.launch_energy(job.handle, self._stream())
+            if job.phase == "sampling" and job.inflight is None and job.steps_done >= job.target:
+                if job.req.kind == "run" and job.epoch < job.req.nepoch:
+                    job.phase = "grad"
+                    job.inflight = self.ex.launch_epoch(job.handle, job.epoch, self._stream())
+                else:
+                    job.phase = "energy"
+                    job.inflight = self.ex.launch_energy(job.handle, self._stream())
         return out
 
     def _admit(self):
@@ -186,18 +210,19 @@ class Scheduler:
             handle, key = self.ex.admit(req)
             self.used += fp
             self._order += 1
-            self.active.append(_Job(req, key, fp, self.clock(), handle=handle, order=self._order))
+            self.active.append(_Job(req, key, fp, self.clock(), handle=handle, order=self._order,
+                                    target=req.nstep))
 
     def _launch(self):
         ready = {}
         for job in self.active:
-            if job.phase == "sampling" and job.inflight is None and job.steps_done < job.req.nstep:
+            if job.phase == "sampling" and job.inflight is None and job.steps_done < job.target:
                 ready.setdefault(job.key, []).append(job)
         for key, jobs in ready.items():
             jobs.sort(key=lambda j: j.order)
             for i in range(0, len(jobs), MAX_BATCH):
                 chunk = jobs[i:i + MAX_BATCH]
-                steps = [min(self.slice_steps, j.req.nstep - j.steps_done) for j in chunk]
+                steps = [min(self.slice_steps, j.target - j.steps_done) for j in chunk]
                 token = self.ex.launch_slice([j.handle for j in chunk],
                                              [j.steps_done for j in chunk], steps, self._stream())
                 self.launches += 1
@@ -265,10 +290,15 @@ class GPUExecutor:
             self._sizes[k] = (call, wf)
         call, _ = self._sizes[k]
         nw = req.nwalkers
-        return int(nw * 3 * mol.nelec * 8                      # positions
-                   + self.lib.qmc_metropolis_scratch_bytes(call.ref, nw)
-                   + self.lib.qmc_scratch_bytes(call.ref, nw, 1)  # local energy
-                   + nw * 8 + self.lib.qmc_reduce_scratch_bytes(nw) + 64)
+        fp = (nw * 3 * mol.nelec * 8                      # positions
+              + self.lib.qmc_metropolis_scratch_bytes(call.ref, nw)
+              + self.lib.qmc_scratch_bytes(call.ref, nw, 1)  # local energy
+              + nw * 8 + self.lib.qmc_reduce_scratch_bytes(nw) + 64)
+        if req.kind == "run":  # psi adjoint, psi / weights, parameters with Adam state
+            nparam = sum(p.numel() for p in self._sizes[k][1].parameters())
+            fp += (self.lib.qmc_adjoint_scratch_bytes(call.ref, nw) + 4 * nw * 8
+                   + 4 * nparam * 8 + req.nepoch * 8)
+        return int(fp)
 
     def admit(self, req):
         torch = self.torch
@@ -286,6 +316,10 @@ class GPUExecutor:
             "red_scr": self.rt.scratch(self.lib.qmc_reduce_scratch_bytes(nw), self.device),
             "stats": torch.empty(3, dtype=torch.float64, device=self.device),
         }
+        if req.kind == "run":
+            h["opt"] = torch.optim.Adam(wf.parameters(), lr=req.lr)
+            h["energies"] = torch.zeros(max(req.nepoch, 1), dtype=torch.float64,
+                                        device=self.device)
         # positions are written on the default stream; the pool streams wait for them
         h["ready"] = torch.cuda.Event()
         h["ready"].record(torch.cuda.current_stream(self.device))
@@ -341,6 +375,33 @@ class GPUExecutor:
         h["host_stats"] = torch.empty(3, dtype=torch.float64, pin_memory=True)
         with torch.cuda.stream(stream):
             h["host_stats"].copy_(h["stats"], non_blocking=True)
+            if h["req"].kind == "run":
+                h["host_energies"] = torch.empty(h["energies"].numel(), dtype=torch.float64,
+                                                 pin_memory=True)
+                h["host_energies"].copy_(h["energies"], non_blocking=True)
+        ev = torch.cuda.Event()
+        ev.record(stream)
+        h["ready"] = ev
+        return ev
+
+    def launch_epoch(self, h, epoch, sid):
+        """One optimisation epoch (solver.py:266-350 with the manual gradient
+        of solver.py:372-431): gradient of the energy on the current walkers,
+        Adam step; all on the job's stream, no host synchronisation."""
+        torch = self.torch
+        stream = self.streams[sid]
+        stream.wait_event(h["ready"])
+        wf, x, opt = h["wf"], h["x"], h["opt"]
+        with torch.cuda.stream(stream):
+            opt.zero_grad()
+            with torch.no_grad():
+                eloc = wf.local_energy(x).reshape(-1)
+            psi = wf(x).reshape(-1)
+            emean = eloc.mean()
+            weight = (eloc - emean) / psi.detach() * (2.0 / psi.numel())
+            psi.backward(weight)
+            opt.step()
+            h["energies"][epoch].copy_(emean)
         ev = torch.cuda.Event()
         ev.record(stream)
         h["ready"] = ev
@@ -350,7 +411,11 @@ class GPUExecutor:
         return token.query()
 
     def stats(self, h):
-        return tuple(float(v) for v in h["host_stats"].tolist())
+        e, v, err = (float(v) for v in h["host_stats"].tolist())
+        energies = None
+        if h["req"].kind == "run":
+            energies = [float(v) for v in h["host_energies"].tolist()][: h["req"].nepoch]
+        return e, v, err, energies
 
     def release(self, h):
         h.clear()

@@ -35,7 +35,7 @@ def test_mixed_against_reference_values(name):
     assert np.max(np.abs(psi - ref) / np.abs(ref)) <= 1e-4
     kin = wf.kinetic_energy(x).cpu().numpy().ravel()
     assert np.max(np.abs(kin - d["kinetic"].ravel()) / np.abs(d["kinetic"].ravel())) <= 2e-4
-    el = wf.local_energy(x).cpu().numpy().ravel()
+    el = wf.local_energy(x).detach().cpu().numpy().ravel()
     assert np.max(np.abs(el - d["eloc"].ravel())) <= 5e-3
     pdf = wf.pdf(x).cpu().numpy()
     assert np.max(np.abs(pdf - d["pdf"]) / np.abs(d["pdf"])) <= 2e-4
@@ -61,8 +61,9 @@ def test_mixed_mean_local_energy_on_fixed_positions():
         s.advance(wf64.pdf, x, nstep=10)
         snaps.append(x.clone())
     X = torch.cat(snaps)[:100000]
-    e64 = wf64.local_energy(X).double()
-    em = wfm.local_energy(X).double()
+    with torch.no_grad():
+        e64 = wf64.local_energy(X).double()
+        em = wfm.local_energy(X).double()
     assert abs(float(em.mean() - e64.mean())) < 1e-5
     with torch.no_grad():
         psi_err = ((wfm(X) - wf64(X)) / wf64(X)).abs()
@@ -103,8 +104,9 @@ def test_batch_size_does_not_change_results(precision):
     small = big[:64].clone()
     with torch.no_grad():
         np.testing.assert_array_equal(wf(small).cpu().numpy(), wf(big)[:64].cpu().numpy())
-    np.testing.assert_array_equal(wf.local_energy(small).cpu().numpy(),
-                                  wf.local_energy(big)[:64].cpu().numpy())
+    with torch.no_grad():
+        np.testing.assert_array_equal(wf.local_energy(small).cpu().numpy(),
+                                      wf.local_energy(big)[:64].cpu().numpy())
     outs = []
     for x in (small, big):
         s = Metropolis(nwalkers=len(x), nstep=30, step_size=0.2, nelec=10,

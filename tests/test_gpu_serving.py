@@ -159,9 +159,42 @@ def test_single_point_equals_sampling_by_hand():
     s = Metropolis(nwalkers=r.nwalkers, nstep=r.nstep, step_size=r.step_size, nelec=mol.nelec,
                    init=mol.domain("atomic"), cuda=True, seed=r.seed)
     s.advance(wf.pdf, x, nstep=r.nstep)
-    el = wf.local_energy(x).reshape(-1).cpu().numpy()
+    el = wf.local_energy(x).reshape(-1).detach().cpu().numpy()
     m = math.fsum(el) / len(el)
     var = float(np.var(el, ddof=1))
     assert abs(res.energy - m) <= 1e-14 * abs(m)
     assert abs(res.variance - var) <= 1e-10 * var
     assert abs(res.error - math.sqrt(var / len(el))) <= 1e-10 * math.sqrt(var / len(el))
+
+
+def test_run_request_is_the_same_alone_and_in_the_mix():
+    """VMC-run jobs (gradient through the psi adjoint with a fixed-order
+    reduction, Adam, resampling) are bitwise reproducible: alone and among
+    single points of other sizes give the same epoch energies and result."""
+    import copy
+
+    from qmctorch_gb300.serving import Request, VMCServer, hydrogen_chain, single_point
+    run = Request(atoms=hydrogen_chain(4, 0.95), nwalkers=1536, nstep=80, seed=21, kind="run",
+                  nepoch=6, lr=1e-2, nstep_update=20)
+    others = [r for r in _requests()[:5]]
+    srv = VMCServer(hbm_budget=1 << 30, slice_steps=32)
+    srv.submit(copy.copy(others[0]))
+    rid = srv.submit(copy.copy(run))
+    srv.poll()
+    for r in others[1:]:
+        srv.submit(copy.copy(r))
+    srv.run()
+    mixed = srv.results[rid]
+    alone = single_point(copy.copy(run))
+    assert mixed.energies == alone.energies and len(mixed.energies) == 6
+    assert (mixed.energy, mixed.variance, mixed.error) == (alone.energy, alone.variance,
+                                                            alone.error)
+
+
+def test_run_request_lowers_the_energy():
+    from qmctorch_gb300.serving import Request, hydrogen_chain, single_point
+    r = Request(atoms=hydrogen_chain(4, 1.0), nwalkers=4096, nstep=200, seed=3, kind="run",
+                nepoch=20, lr=2e-2, nstep_update=25, precision="fp64")
+    res = single_point(r)
+    e = np.asarray(res.energies)
+    assert np.all(np.isfinite(e)) and e[-5:].mean() < e[:5].mean()

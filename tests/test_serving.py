@@ -51,13 +51,18 @@ class FakeExecutor:
     def launch_energy(self, h, sid):
         return self._token()
 
+    def launch_epoch(self, h, epoch, sid):
+        h.setdefault("epochs", []).append(epoch)
+        return self._token()
+
     def ready(self, token):
         token.tick()
         return token.left <= 0
 
     def stats(self, h):
         r = h["req"]
-        return (float(r.seed), float(r.nwalkers), float(r.nstep))
+        energies = [float(e) for e in h.get("epochs", [])] if r.kind == "run" else None
+        return (float(r.seed), float(r.nwalkers), float(r.nstep), energies)
 
     def release(self, h):
         r = h["req"]
@@ -151,3 +156,29 @@ def test_jobs_arriving_later_start_while_others_run():
     assert 0 not in s.results
     s.run(sleep=0)
     assert set(s.results) == {0, 1}
+
+
+def test_run_jobs_alternate_gradient_and_resampling():
+    """kind="run": initial sampling, then nepoch x (gradient, nstep_update
+    resampling steps), then the final energy; single points run alongside."""
+    ex = FakeExecutor()
+    s = Scheduler(ex, hbm_budget=10 ** 9, slice_steps=40)
+    r = req(4, 10, 100)
+    r.kind, r.nepoch, r.nstep_update = "run", 3, 25
+    s.submit(r)
+    s.submit(req(4, 10, 60))
+    s.run(sleep=0)
+    res = s.results[0]
+    assert res.energies == [0.0, 1.0, 2.0]
+    per = [(o, n) for rids, offs, steps in ex.slices for rr, o, n in zip(rids, offs, steps)
+           if rr == 0]
+    assert per == [(0, 40), (40, 40), (80, 20), (100, 25), (125, 25), (150, 25)]
+    assert s.results[1].energies is None
+
+
+def test_unknown_request_kind_is_rejected():
+    s = Scheduler(FakeExecutor(), hbm_budget=10 ** 9)
+    r = req(2, 10, 10)
+    r.kind = "optimise"
+    with pytest.raises(ValueError):
+        s.submit(r)
