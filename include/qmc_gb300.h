@@ -225,6 +225,16 @@ int qmc_wf_psi_adjoint(const qmc_wf_desc* d, const double* pos, int64_t nwalkers
                        double* grad_exp, double* grad_W, int32_t ldw, double* grad_jastrow_w,
                        double* grad_ci, void* scratch, int64_t scratch_bytes, void* stream);
 
+/*
+ * Electron-position gradients: grad[w][3*i + q] = d psi / d r_iq (pdf = 0) or
+ * d psi^2 / d r_iq = 2 psi d psi / d r_iq (pdf != 0), by the Jacobi formula,
+ * FP64. Replaces SlaterJastrow.gradients_jacobi (slater_jastrow.py:346-447),
+ * used by WaveFunction.pdf(pos, return_grad=True) (wf_base.py:241-247).
+ */
+int64_t qmc_grad_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
+int qmc_wf_gradients(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, int32_t pdf,
+                     double* grad, void* scratch, int64_t scratch_bytes, void* stream);
+
 /* Scratch bytes for qmc_wf_local_energy_adjoint. */
 int64_t qmc_eloc_adjoint_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
 

@@ -526,6 +526,161 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
   }
 }
 
+// ---------------------------------------------------------------------------
+// Electron-position gradients of psi (Jacobi formula)
+// ---------------------------------------------------------------------------
+// grad_i psi = J grad_i Sigma + J grad_i U Sigma with Sigma = sum_k c_k D_k and
+// grad_i Sigma = sum_k c_k D_k Tr(A_u^-1 grad_i A_u) over the determinant u of
+// electron i's spin; only row i of grad_i A_u is non-zero, so the trace is
+// sum_j (A_u^-1)[j][i] grad MO_cols[j](r_i) (slater_jastrow.py:346-447).
+struct GradLayout {
+  int64_t aov, aox, aoy, aoz, ma, mx, my, mz, lu, x, dv, gd, total;
+};
+
+__host__ __device__ inline GradLayout grad_layout(const qmc_wf_desc& d) {
+  GradLayout L;
+  const int64_t ne = d.nelec, nao = d.nao, nmu = d.nmo_used;
+  const int64_t nmax = d.nup > d.ndown ? d.nup : d.ndown, nd = d.ndet[0] + d.ndet[1];
+  int64_t o = 0;
+  auto take = [&](int64_t n) {
+    const int64_t r = o;
+    o += n;
+    return r;
+  };
+  L.aov = take(ne * nao);
+  L.aox = take(ne * nao);
+  L.aoy = take(ne * nao);
+  L.aoz = take(ne * nao);
+  L.ma = take(ne * nmu);
+  L.mx = take(ne * nmu);
+  L.my = take(ne * nmu);
+  L.mz = take(ne * nmu);
+  L.lu = take(nmax * nmax);
+  L.x = take(nmax * nmax);
+  L.dv = take(nd);
+  L.gd = take(nd * nmax * 3);  // per determinant: d log D_u / d r_i for its spin's electrons
+  L.total = o;
+  return L;
+}
+
+__global__ void __launch_bounds__(kAdjTPB) grad_kernel(const qmc_wf_desc d,
+                                                       const double* __restrict__ pos, int64_t nw,
+                                                       int pdf, double* __restrict__ out,
+                                                       double* __restrict__ scr, int64_t ss) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ncol = round_up(d.nmo_used, 8);
+  const Tables<double> t = load_tables<double>(d, d.nmo_used, ncol, smem);
+  const int nmu = d.nmo_used, ne = d.nelec, nao = d.nao;
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  const GradLayout L = grad_layout(d);
+  double* sw = scr + w;
+  auto R2 = [&](int64_t base, int e, int k, int n) -> double& {
+    return sw[(base + (int64_t)e * n + k) * ss];
+  };
+  const PosView P{pos + w * 3 * ne, 1};
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  // Jastrow: U and grad_i U
+  double logj = 0.0;
+  double* o = out + w * 3 * ne;
+  for (int i = 0; i < 3 * ne; ++i) o[i] = 0.0;
+  const double wj = __ldg(d.jastrow_w);
+  // AO values and gradients, MO rows
+  for (int e = 0; e < ne; ++e) {
+    for_each_ao<double, true>(t, P(3 * e), P(3 * e + 1), P(3 * e + 2),
+                              [&](int a, const AOVal<double>& v) {
+                                R2(L.aov, e, a, nao) = v.v;
+                                R2(L.aox, e, a, nao) = v.gx;
+                                R2(L.aoy, e, a, nao) = v.gy;
+                                R2(L.aoz, e, a, nao) = v.gz;
+                              });
+    for (int j = 0; j < nmu; ++j) {
+      double sa = 0.0, sx = 0.0, sy = 0.0, sz = 0.0;
+      for (int a = 0; a < nao; ++a) {
+        const double wv = t.W[(int64_t)a * t.ncol + j];
+        sa = fma(R2(L.aov, e, a, nao), wv, sa);
+        sx = fma(R2(L.aox, e, a, nao), wv, sx);
+        sy = fma(R2(L.aoy, e, a, nao), wv, sy);
+        sz = fma(R2(L.aoz, e, a, nao), wv, sz);
+      }
+      R2(L.ma, e, j, nmu) = sa;
+      R2(L.mx, e, j, nmu) = sx;
+      R2(L.my, e, j, nmu) = sy;
+      R2(L.mz, e, j, nmu) = sz;
+    }
+  }
+  // determinants and d log D_u / d r_i
+  MView<double> LU{sw + L.lu * ss, (int64_t)nmax * ss, ss};
+  MView<double> X{sw + L.x * ss, (int64_t)nmax * ss, ss};
+  double* DV = sw + L.dv * ss;
+  int piv[QMC_MAX_NSPIN], cols[QMC_MAX_NSPIN];
+  for (int s = 0; s < 2; ++s) {
+    const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0;
+    for (int u = 0; u < d.ndet[s]; ++u) {
+      const int k = (s ? d.ndet[0] : 0) + u;
+      double det = 1.0;
+      if (n > 0) {
+        det_columns(d, s, u, cols);
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) LU(i, j) = R2(L.ma, r0 + i, cols[j], nmu);
+        det = lu_factor<double>(LU, n, piv);
+        for (int i = 0; i < n; ++i)
+          for (int j = 0; j < n; ++j) X(i, j) = i == j ? 1.0 : 0.0;
+        lu_solve<double>(LU, n, piv, X.c(), X, n);
+        for (int i = 0; i < n; ++i) {
+          double gx = 0.0, gy = 0.0, gz = 0.0;
+          for (int j = 0; j < n; ++j) {
+            const double xv = X(j, i);
+            gx = fma(xv, R2(L.mx, r0 + i, cols[j], nmu), gx);
+            gy = fma(xv, R2(L.my, r0 + i, cols[j], nmu), gy);
+            gz = fma(xv, R2(L.mz, r0 + i, cols[j], nmu), gz);
+          }
+          sw[(L.gd + ((int64_t)k * nmax + i) * 3 + 0) * ss] = gx;
+          sw[(L.gd + ((int64_t)k * nmax + i) * 3 + 1) * ss] = gy;
+          sw[(L.gd + ((int64_t)k * nmax + i) * 3 + 2) * ss] = gz;
+        }
+      }
+      DV[k * ss] = det;
+    }
+  }
+  auto dvk = [&](int s, int u) { return DV[((s ? d.ndet[0] : 0) + u) * ss]; };
+  double sigma = 0.0;
+  for (int k = 0; k < d.ncfg; ++k) {
+    const int uu = __ldg(d.cfg_det[0] + k), ud = __ldg(d.cfg_det[1] + k);
+    const double cd = __ldg(d.ci_weight + k) * dvk(0, uu) * dvk(1, ud);
+    sigma += cd;
+    for (int s = 0; s < 2; ++s) {
+      const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0;
+      const int kk = s ? d.ndet[0] + ud : uu;
+      for (int i = 0; i < n; ++i)
+        for (int q = 0; q < 3; ++q)
+          o[3 * (r0 + i) + q] = fma(cd, sw[(L.gd + ((int64_t)kk * nmax + i) * 3 + q) * ss],
+                                    o[3 * (r0 + i) + q]);
+    }
+  }
+  // Jastrow: grad_i U (Pade kernel K' = w0 / (1 + w r)^2) and psi = J Sigma
+  double J = 1.0;
+  if (d.use_jastrow) {
+    for (int i = 0; i < ne; ++i) {
+      double g[3] = {0.0, 0.0, 0.0};
+      for (int j = 0; j < ne; ++j) {
+        if (j == i) continue;
+        const double dx[3] = {P(3 * i) - P(3 * j), P(3 * i + 1) - P(3 * j + 1),
+                              P(3 * i + 2) - P(3 * j + 2)};
+        const double r = sqrt(dx[0] * dx[0] + dx[1] * dx[1] + dx[2] * dx[2]);
+        const double w0 = same_spin(d, i, j) ? 0.25 : 0.5;
+        const double u = 1.0 / (1.0 + wj * r);
+        if (j > i) logj += w0 * r * u;
+        for (int q = 0; q < 3; ++q) g[q] += w0 * u * u * dx[q] / r;
+      }
+      for (int q = 0; q < 3; ++q) o[3 * i + q] = fma(g[q], sigma, o[3 * i + q]);
+    }
+    J = exp(logj);
+  }
+  const double scale = pdf ? 2.0 * J * J * sigma : J;  // grad psi or grad psi^2 = 2 psi grad psi
+  for (int i = 0; i < 3 * ne; ++i) o[i] *= scale;
+}
+
 // Sum of parameter i's walker slots in a fixed order (per-thread strided
 // partial sums, then a fixed tree), added to its output: W (row stride ldw),
 // exponents, CI weights, Pade weight. One block per parameter.
@@ -632,6 +787,31 @@ int qmc_wf_local_energy_adjoint(const qmc_wf_desc* d0, const double* pos, int64_
   adj_reduce_kernel<<<(unsigned)adj_acc_doubles(dd), kRedTPB, 0, cs>>>(
       gacc, nw, ss, dd.nao, dd.nmo_used, dd.nweight, nentries, dd.ncfg, grad_W, ldw, grad_exp,
       grad_ci, d->use_jastrow ? grad_jastrow_w : nullptr);
+  return launch_status();
+}
+
+int64_t qmc_grad_scratch_bytes(const qmc_wf_desc* d, int64_t nw) {
+  if (check_desc(d) != QMC_OK || nw < 0) return -1;
+  return grad_layout(*d).total * pad_walkers(nw) * (int64_t)sizeof(double);
+}
+
+int qmc_wf_gradients(const qmc_wf_desc* d0, const double* pos, int64_t nw, int32_t pdf,
+                     double* grad, void* scratch, int64_t scratch_bytes, void* stream) {
+  int st = check_desc(d0);
+  if (st) return st;
+  qmc_wf_desc dd = *d0;
+  dd.precision = QMC_PREC_FP64;
+  const qmc_wf_desc* d = &dd;
+  if (nw < 0) return QMC_ERR_ARG;
+  if (nw == 0) return QMC_OK;
+  if (!pos || !grad || !scratch) return QMC_ERR_ARG;
+  if (scratch_bytes < qmc_grad_scratch_bytes(d, nw)) return QMC_ERR_SCRATCH;
+  const int ncol = round_up(d->nmo_used, 8);
+  const int64_t smem = tables_smem_bytes<double>(*d, ncol);
+  if ((st = prepare_smem(grad_kernel, smem))) return st;
+  const dim3 grid((unsigned)((nw + kAdjTPB - 1) / kAdjTPB));
+  grad_kernel<<<grid, kAdjTPB, smem, (cudaStream_t)stream>>>(dd, pos, nw, pdf ? 1 : 0, grad,
+                                                             (double*)scratch, pad_walkers(nw));
   return launch_status();
 }
 

@@ -304,8 +304,22 @@ class SlaterJastrow(WaveFunction):
     kinetic_energy_autograd = kinetic_energy_jacobi
 
     def gradients_jacobi(self, x, sum_grad=False, pdf=False):
-        raise NotImplementedError("wave-function gradients with respect to the electron "
-                                  "positions are not on the GB300 path yet")
+        """d psi / d r (or d psi^2 / d r with pdf=True) -> (nbatch, 3*nelec), by
+        the Jacobi formula (slater_jastrow.py:346-447); FP64. ``sum_grad`` is
+        accepted and, as in the reference, not used."""
+        device = rt.cuda_device()
+        xd = rt.dev64(x, device).reshape(-1, self.ndim_tot)
+        nb = xd.shape[0]
+        call = self._desc(device)
+        lib = _lib.lib()
+        scr = rt.scratch(lib.qmc_grad_scratch_bytes(call.ref, nb), device)
+        out = torch.empty((nb, self.ndim_tot), dtype=rt.F64, device=device)
+        _lib.check(lib.qmc_wf_gradients(call.ref, rt.ptr(xd), nb, 1 if pdf else 0, rt.ptr(out),
+                                        rt.ptr(scr), scr.numel(), rt.stream_handle()),
+                   "qmc_wf_gradients")
+        return out.to(device=x.device, dtype=x.dtype)
+
+    gradients_autograd = gradients_jacobi
 
     def _potentials(self, pos, en=True, ee=True):
         device = rt.cuda_device()

@@ -9,7 +9,8 @@ Writes ``tests/golden/<case>.npz``. Each file holds the molecule / basis
 namespace (``mol_*`` / ``basis_*`` keys, the layout of
 ``qmctorch_gb300.scf.Molecule.save``), the seeded walker positions and the
 reference outputs: AO values and derivatives, MOs, Jastrow factor and
-derivatives, Slater determinants, psi, pdf, kinetic and local energies, a
+derivatives, Slater determinants, psi, pdf, their electron-position
+gradients (gradients_jacobi), kinetic and local energies, a
 Metropolis replay with injected proposals and uniforms, and the parameter
 gradients of the manual and automatic VMC energy gradients.
 """
@@ -98,6 +99,8 @@ def main(reference_root, only=()):
                 data.update(jast=jast.numpy(), djast=djast.numpy(), d2jast=d2jast.numpy(),
                             djast_sum=wf.jastrow(pos, derivative=1).numpy(),
                             dets=wf.pool(wf.mo(ao)).numpy())
+            data.update(grad_psi=wf.gradients_jacobi(pos).numpy(),
+                        grad_pdf=wf.gradients_jacobi(pos, pdf=True).numpy())
             data.update(psi=wf(pos).numpy(), pdf=wf.pdf(pos).numpy(),
                         kinetic=wf.kinetic_energy(pos).numpy(),
                         eloc=wf.local_energy(pos).numpy(),

@@ -47,6 +47,18 @@ def test_psi_and_local_energy(name):
     assert abs(wf.nuclear_repulsion() - float(d["v_nn"])) < 1e-12 * max(1, abs(float(d["v_nn"])))
 
 
+@pytest.mark.parametrize("name", CASES)
+def test_position_gradients(name):
+    """gradients_jacobi and pdf(return_grad=True) against the reference's
+    gradients_jacobi (slater_jastrow.py:346-447) on the golden positions."""
+    mol, d = load(name)
+    wf = make_wf(mol, d)
+    pos = torch.as_tensor(d["pos"]).cuda()
+    close(wf.gradients_jacobi(pos), d["grad_psi"])
+    close(wf.gradients_jacobi(pos, pdf=True), d["grad_pdf"])
+    close(wf.pdf(pos, return_grad=True), d["grad_pdf"])
+
+
 @pytest.mark.parametrize("name", [c for c in CASES if c != "c6h6"])
 def test_staged_modules(name):
     mol, d = load(name)
