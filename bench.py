@@ -63,6 +63,9 @@ def parse():
     p.add_argument("--serve-requests", type=int, default=48)
     p.add_argument("--serve-rates", type=float, nargs="*", default=[10.0, 40.0, 160.0])
     p.add_argument("--serve-budget-gb", type=int, default=32)
+    p.add_argument("--skip", default="",
+                   help="comma list of sections to leave out (c6h6, serving, small, modules, "
+                        "precision, e2e); for short profiling runs")
     p.add_argument("--c6h6-sweeps", type=int, default=4,
                    help="all-elec-iter sweeps per timed C6H6 launch (mixed method)")
     p.add_argument("--mc-steps", type=int, default=100)
@@ -535,13 +538,17 @@ def run_gb300(args):
         el_s = _timed(torch, el_call, args.steps, flush)
         results[name] = {"met_s": met_s, "el_s": el_s,
                          "accept": float(acc.sum()) / (nw * args.mc_steps * args.steps)}
-    c6h6 = bench_c6h6(torch, lib, args, device, flush, rank) if args.c6h6_walkers > 0 else None
+    skip = set(filter(None, args.skip.split(",")))
+    c6h6 = (bench_c6h6(torch, lib, args, device, flush, rank)
+            if args.c6h6_walkers > 0 and "c6h6" not in skip else None)
     clk = clocks.stop()
-    serving = bench_serving(args) if (args.serve_requests > 0 and rank == 0) else None
-    small = bench_h2_lih(torch, device) if rank == 0 else None
-    staged = bench_staged(torch, wf64, x_eq, flush) if rank == 0 else None
+    serving = (bench_serving(args) if (args.serve_requests > 0 and rank == 0
+                                       and "serving" not in skip) else None)
+    small = bench_h2_lih(torch, device) if rank == 0 and "small" not in skip else None
+    staged = bench_staged(torch, wf64, x_eq, flush) if rank == 0 and "modules" not in skip else None
 
-    prec = precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank)) if rank == 0 else None
+    prec = (precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank))
+            if rank == 0 and "precision" not in skip else None)
 
     # --- end to end through the public API (mixed method), host buffers ---
     pos_host = x_eq.detach().cpu().pin_memory()
