@@ -457,6 +457,16 @@ def bench_serving(args):
     return out
 
 
+def slowest_rank_times(torch, vals, device, world):
+    """Per-quantity maximum of the ranks' timed durations (replicas: every
+    rank runs its own walkers, the job takes as long as the slowest rank)."""
+    loc = torch.tensor(vals, dtype=torch.float64, device=device)
+    if world > 1:
+        import torch.distributed as dist
+        dist.all_reduce(loc, op=dist.ReduceOp.MAX)
+    return loc.tolist()
+
+
 def run_gb300(args):
     import ctypes
 
@@ -564,12 +574,9 @@ def run_gb300(args):
     h2d = pos_host.numel() * 8
     d2h = out.numel() * out.element_size() + pos_host.numel() * 8
 
-    vals = [results["mixed"]["met_s"], results["mixed"]["el_s"], results["fp64"]["met_s"],
-            results["fp64"]["el_s"], e2e_s]
-    loc = torch.tensor(vals, dtype=torch.float64, device=device)
-    if world > 1:
-        dist.all_reduce(loc, op=dist.ReduceOp.MAX)
-    m_met, m_el, f_met, f_el, e2e_s = loc.tolist()
+    m_met, m_el, f_met, f_el, e2e_s = slowest_rank_times(
+        torch, [results["mixed"]["met_s"], results["mixed"]["el_s"], results["fp64"]["met_s"],
+                results["fp64"]["el_s"], e2e_s], device, world)
     units = nw * args.mc_steps * args.steps
     value = units * world / m_met
     if rank == 0:

@@ -160,3 +160,39 @@ def test_missing_gpu_fails_loudly():
     wf = SlaterJastrow(mol)
     with pytest.raises(RuntimeError, match="CUDA"):
         wf(torch.zeros(2, 6))
+
+
+@pytest.mark.parametrize("name", ["h2o_sd", "lih_cas"])
+def test_new_entry_points_reject_bad_arguments_without_a_gpu(name):
+    """Batch Metropolis, statistics, position gradients and the local-energy
+    adjoint report argument errors before touching the device."""
+    lib = _lib.lib()
+    desc, keep, wf = _desc_for(name)
+    args = (_lib.MetropolisArgs * 2)()
+    descs = (_lib.WfDesc * 2)(desc, desc)
+    scr = (ctypes.c_void_p * 2)(ctypes.c_void_p(8), ctypes.c_void_p(8))
+    nb = (ctypes.c_int64 * 2)(1 << 40, 1 << 40)
+    assert lib.qmc_metropolis_run_batch(descs, args, scr, nb, 0, None) == 1
+    assert lib.qmc_metropolis_run_batch(descs, args, scr, nb, 33, None) == 1
+    for a in args:
+        a.nwalkers, a.nstep, a.ndecor, a.pos = 4, 1, 1, ctypes.c_void_p(8)
+    args[1].move_type = 2  # single-electron moves are not batched
+    assert lib.qmc_metropolis_run_batch(descs, args, scr, nb, 2, None) == 5
+    args[1].move_type = 0
+    descs[1].precision = 1 - descs[0].precision
+    assert lib.qmc_metropolis_run_batch(descs, args, scr, nb, 2, None) == 2
+    assert lib.qmc_reduce_stats(ctypes.c_void_p(8), 0, ctypes.c_void_p(8), ctypes.c_void_p(8), 64,
+                                None) == 1
+    assert lib.qmc_reduce_stats(ctypes.c_void_p(8), 10 ** 6, ctypes.c_void_p(8),
+                                ctypes.c_void_p(8), 8, None) == 3
+    assert lib.qmc_reduce_scratch_bytes(10 ** 6) > lib.qmc_reduce_scratch_bytes(10)
+    assert lib.qmc_wf_gradients(ctypes.byref(desc), None, -1, 0, None, None, 0, None) == 1
+    assert lib.qmc_wf_gradients(ctypes.byref(desc), ctypes.c_void_p(8), 10, 0, ctypes.c_void_p(8),
+                                ctypes.c_void_p(8), 8, None) == 3
+    gb = lib.qmc_eloc_adjoint_scratch_bytes(ctypes.byref(desc), 100)
+    assert gb > lib.qmc_adjoint_scratch_bytes(ctypes.byref(desc), 100) > 0
+    v = ctypes.c_void_p(8)
+    assert lib.qmc_wf_local_energy_adjoint(ctypes.byref(desc), v, 10, v, v, 1, v, v, 0, v, v, v,
+                                           gb, None) == 1  # ldw < nmo_used
+    assert lib.qmc_wf_local_energy_adjoint(ctypes.byref(desc), v, 10, v, v, 1, v, v,
+                                           desc.nmo_used, v, v, v, 8, None) == 3
