@@ -37,6 +37,9 @@ CONFIGS = "single_double(4,4)"
 STEP_SIZE = 0.2
 L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 NWALKERS = 16384
+# DRAM bytes (read + write) of one metropolis_kernel<float> launch on this workload, from
+# ncu (profiles/metropolis_mixed_h2o_ccpvdz_16384w.md); independent of the step count
+TRAFFIC_PER_LAUNCH = 7.32e6
 C6H6 = ("C 1.39 0 0; C 0.695 1.20377 0; C -0.695 1.20377 0; C -1.39 0 0; "
         "C -0.695 -1.20377 0; C 0.695 -1.20377 0; H 2.48 0 0; H 1.24 2.14774 0; "
         "H -1.24 2.14774 0; H -2.48 0 0; H -1.24 -2.14774 0; H 1.24 -2.14774 0")
@@ -584,6 +587,13 @@ def run_gb300(args):
         launch_units = nw * args.mc_steps
         ach_m = flops * launch_units / (m_met / args.steps) / 1e9
         ach_f = flops * launch_units / (f_met / args.steps) / 1e9
+        hbm_alg = 2 * nw * 3 * mol.nelec * 8  # positions in and out, FP64
+        hbm_peak = 6800.0
+        try:
+            with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+                hbm_peak = float(json.load(f).get("hbm_gbs", hbm_peak))
+        except Exception:
+            pass
         line = {
             "metric": METRIC,
             "value": value,
@@ -605,12 +615,22 @@ def run_gb300(args):
             "speedup_vs_fp64": {"walker_steps": f_met / m_met, "el": f_el / m_el},
             "precision_vs_fp64": prec,
             "acceptance": results["mixed"]["accept"],
-            "roofline": {"bound": "fp32", "kernel": "metropolis_kernel<float>",
-                         "achieved": ach_m, "peak": peaks["fp32_gflops"], "unit": "GFLOP/s",
-                         "frac": ach_m / peaks["fp32_gflops"], "traffic": None,
-                         "flops_per_walker_step": flops, "exp_per_walker_step": exps,
-                         "peak_source": "in-run FP32 FMA probe (qmc_probe_fma); "
-                                        "MEASURED_PEAKS.json holds HBM and BF16 figures only"},
+            # HBM roofline of the dominant kernel (schema): algorithmic bytes of one
+            # launch = the walkers' positions read and written once (the state stays
+            # on chip for all mc-steps); traffic = ncu DRAM bytes of one launch
+            "roofline": {"bound": "hbm", "kernel": "metropolis_kernel<float>",
+                         "achieved": hbm_alg / (m_met / args.steps) / 1e9,
+                         "peak": hbm_peak, "unit": "GB/s",
+                         "frac": hbm_alg / (m_met / args.steps) / 1e9 / hbm_peak,
+                         "traffic": TRAFFIC_PER_LAUNCH,
+                         "algorithmic_bytes_per_launch": hbm_alg,
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)",
+                         "note": "not HBM-bound: compute / latency bound, see roofline_fp32"},
+            "roofline_fp32": {"bound": "fp32", "kernel": "metropolis_kernel<float>",
+                              "achieved": ach_m, "peak": peaks["fp32_gflops"], "unit": "GFLOP/s",
+                              "frac": ach_m / peaks["fp32_gflops"],
+                              "flops_per_walker_step": flops, "exp_per_walker_step": exps,
+                              "peak_source": "in-run FP32 FMA probe (qmc_probe_fma of measured)"},
             "roofline_fp64": {"bound": "fp64", "kernel": "metropolis_kernel<double>",
                               "achieved": ach_f, "peak": peaks["fp64_gflops"], "unit": "GFLOP/s",
                               "frac": ach_f / peaks["fp64_gflops"]},

@@ -23,72 +23,6 @@
 
 namespace qmc {
 
-// ---------------------------------------------------------------------------
-// shared-memory and scratch layouts
-// ---------------------------------------------------------------------------
-struct EPShape {
-  int nwb;       // walkers per block
-  int nslot;     // threads per walker in the electron phase (electron e on slot e % nslot)
-  int nthreads;  // threads per block
-  int ncol;      // W columns stored per AO (nmo_used rounded up to the MO chunk)
-  int64_t smem;  // dynamic shared memory bytes
-  int64_t o_tab, o_pos, o_pnew, o_mo, o_bk, o_jrow, o_vrow, o_dref, o_psi, o_f, o_kin, o_v,
-      o_iel, o_acc;
-};
-
-template <typename R>
-__host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb, int jc,
-                                           int nslot) {
-  EPShape s;
-  s.nwb = nwb;
-  s.nslot = nslot;
-  int nt = nwb * nslot;
-  if (nt < 2 * nwb) nt = 2 * nwb;
-  s.nthreads = ((nt + 31) / 32) * 32;
-  s.ncol = round_up(d.nmo_used, jc);
-  const int64_t nc = 3 * (int64_t)d.nelec, nmu = d.nmo_used;
-  const int64_t xps = 2 * (int64_t)sizeof(R);  // bytes of one split coordinate
-  int64_t o = 0;
-  s.o_tab = o;
-  o += tables_smem_bytes<R>(d, s.ncol);
-  o = (o + 15) & ~int64_t(15);
-  s.o_pos = o;
-  o += align8(nwb * nc * xps);
-  s.o_pnew = o;
-  if (kind == 2) o += align8(nwb * nc * xps);
-  s.o_mo = o;
-  o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
-  s.o_bk = o;
-  if (kind == 1) o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
-  s.o_jrow = o;
-  o += align8((int64_t)d.nelec * nwb * 8);
-  s.o_vrow = o;
-  if (kind == 1) o += align8((int64_t)d.nelec * nwb * 8);
-  s.o_dref = o;
-  o += 2 * nwb * 8;
-  s.o_psi = o;
-  o += nwb * 8;
-  s.o_f = o;
-  o += nwb * 8;
-  s.o_kin = o;
-  o += nwb * 8;
-  s.o_v = o;
-  o += nwb * 8;
-  s.o_iel = o;
-  o += align8(nwb * 4);
-  s.o_acc = o;
-  o += align8(nwb * 4);
-  s.smem = o;
-  return s;
-}
-
-// Thread bound of the electron-parallel kernels: 1024 threads (64 registers)
-// for FP32, 512 (128 registers) for FP64, whose accumulators are twice as wide.
-template <typename R>
-struct EPBound {
-  static constexpr int kThreads = kMixed<R> ? 1024 : 512;
-};
-
 // Per-walker scratch: the determinant-phase work arrays of both spins. The
 // relative determinant values are FP64 for the local energy and of the
 // compute type for psi.
@@ -133,6 +67,86 @@ __host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
   L.bytes_per_slot = o;
   return L;
 }
+
+// ---------------------------------------------------------------------------
+// shared-memory and scratch layouts
+// ---------------------------------------------------------------------------
+constexpr int64_t kDetSmemBytes = 16384;
+
+struct EPShape {
+  int nwb;       // walkers per block
+  int nslot;     // threads per walker in the electron phase (electron e on slot e % nslot)
+  int nthreads;  // threads per block
+  int ncol;      // W columns stored per AO (nmo_used rounded up to the MO chunk)
+  int64_t smem;  // dynamic shared memory bytes
+  int64_t o_tab, o_pos, o_pnew, o_mo, o_bk, o_jrow, o_vrow, o_dref, o_psi, o_f, o_kin, o_v,
+      o_iel, o_acc;
+  int64_t o_det;  // determinant-phase work arrays of the block's walkers, or -1: HBM scratch
+};
+
+template <typename R>
+__host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb, int jc,
+                                           int nslot) {
+  EPShape s;
+  s.nwb = nwb;
+  s.nslot = nslot;
+  int nt = nwb * nslot;
+  if (nt < 2 * nwb) nt = 2 * nwb;
+  s.nthreads = ((nt + 31) / 32) * 32;
+  s.ncol = round_up(d.nmo_used, jc);
+  const int64_t nc = 3 * (int64_t)d.nelec, nmu = d.nmo_used;
+  const int64_t xps = 2 * (int64_t)sizeof(R);  // bytes of one split coordinate
+  int64_t o = 0;
+  s.o_tab = o;
+  o += tables_smem_bytes<R>(d, s.ncol);
+  o = (o + 15) & ~int64_t(15);
+  s.o_pos = o;
+  o += align8(nwb * nc * xps);
+  s.o_pnew = o;
+  if (kind == 2) o += align8(nwb * nc * xps);
+  s.o_mo = o;
+  o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
+  s.o_bk = o;
+  if (kind == 1) o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
+  s.o_jrow = o;
+  o += align8((int64_t)d.nelec * nwb * 8);
+  s.o_vrow = o;
+  if (kind == 1) o += align8((int64_t)d.nelec * nwb * 8);
+  s.o_dref = o;
+  o += 2 * nwb * 8;
+  s.o_psi = o;
+  o += nwb * 8;
+  s.o_f = o;
+  o += nwb * 8;
+  s.o_kin = o;
+  o += nwb * 8;
+  s.o_v = o;
+  o += nwb * 8;
+  s.o_iel = o;
+  o += align8(nwb * 4);
+  s.o_acc = o;
+  o += align8(nwb * 4);
+  // the determinant phase works in shared memory when the block's arrays are
+  // small (the psi / Metropolis kernels of small molecules), else in HBM scratch
+  const int64_t det_bytes = (int64_t)nwb * ep_layout(d, kind == 1 ? 1 : 0).bytes_per_slot;
+  if (det_bytes <= kDetSmemBytes) {
+    o = (o + 15) & ~int64_t(15);
+    s.o_det = o;
+    o += det_bytes;
+  } else {
+    s.o_det = -1;
+  }
+  s.smem = o;
+  return s;
+}
+
+// Thread bound of the electron-parallel kernels: 1024 threads (64 registers)
+// for FP32, 512 (128 registers) for FP64, whose accumulators are twice as wide.
+template <typename R>
+struct EPBound {
+  static constexpr int kThreads = kMixed<R> ? 1024 : 512;
+};
+
 
 // ---------------------------------------------------------------------------
 // AO groups
@@ -494,9 +508,13 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   }
   __syncthreads();
   const EPLayout L = ep_layout(d, KIN ? 1 : 0);
+  const bool dsm = S.o_det >= 0;  // work arrays in shared memory: slot = local walker
+  unsigned char* const dbase = dsm ? p.smem + S.o_det : scr;
+  const int64_t dss = dsm ? nwb : ss;
   if (tid < 2 * nwb) {
     const int spin = tid / nwb, wl = tid - spin * nwb;
-    if (w0 + wl < nw) ep_det<R, KIN>(d, L, scr, ss, w0 + wl, spin, MO, BK, wl, nwb, DREF);
+    if (w0 + wl < nw)
+      ep_det<R, KIN>(d, L, dbase, dss, dsm ? wl : w0 + wl, spin, MO, BK, wl, nwb, DREF);
   }
   __syncthreads();
   if (tid < nwb && w0 + tid < nw) {
@@ -504,9 +522,10 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
     const int wl = tid;
     const int64_t w = w0 + wl;
     double kin = 0.0;
-    const T* dv = rptr<T>(scr, L.dv, ss, w);
-    const double* ov = KIN ? rptr<double>(scr, L.ov, ss, w) : nullptr;
-    const double psid = ci_combine<T, KIN, T>(d, dv, ov, ss, DREF[wl], DREF[nwb + wl], &kin);
+    const int64_t slot = dsm ? wl : w;
+    const T* dv = rptr<T>(dbase, L.dv, dss, slot);
+    const double* ov = KIN ? rptr<double>(dbase, L.ov, dss, slot) : nullptr;
+    const double psid = ci_combine<T, KIN, T>(d, dv, ov, dss, DREF[wl], DREF[nwb + wl], &kin);
     double logj = 0.0, v = 0.0;
     for (int e = 0; e < ne; ++e) {
       logj += JR[e * nwb + wl];
