@@ -144,7 +144,8 @@ class ClockSampler:
     def __init__(self, index):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", "clocks_rank%d.csv" % index)
+        outdir = os.environ.get("QMC_BENCH_OUT", os.path.join(ROOT, "bench_out"))
+        self.path = os.path.join(outdir, "clocks_rank%d.csv" % index)
 
     def start(self):
         try:
@@ -349,6 +350,18 @@ def bench_c6h6(torch, lib, args, device, flush, rank):
     out["speedup_mixed_vs_fp64"] = {
         "walker_sweeps": out["mixed"]["walker_sweeps_per_s"] / out["fp64"]["walker_sweeps_per_s"],
         "el": out["mixed"]["el_per_s"] / out["fp64"]["el_per_s"]}
+    # precision of the mixed method on the positions the chains reached
+    with torch.no_grad():
+        e64 = wfs["fp64"].local_energy(x).reshape(-1)
+        em = wfs["mixed"].local_energy(x).reshape(-1)
+        de = (em - e64).abs()
+        out["precision_vs_fp64"] = {
+            "n_positions": int(x.shape[0]),
+            "mean_eloc_fp64": float(e64.mean()), "mean_eloc_mixed": float(em.mean()),
+            "mean_eloc_diff_ha": float((em - e64).mean()),
+            "eloc_abs_err_median_ha": float(de.median()),
+            "eloc_abs_err_p99_ha": float(torch.quantile(de[:min(len(de), 1 << 20)], 0.99)),
+            "stat_error_of_mean_ha": float(e64.std() / len(e64) ** 0.5)}
     return out
 
 
