@@ -39,7 +39,7 @@ L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
 NWALKERS = 16384
 # DRAM bytes (read + write) of one metropolis_kernel<float> launch on this workload, from
 # ncu (profiles/metropolis_mixed_h2o_ccpvdz_16384w.md); independent of the step count
-TRAFFIC_PER_LAUNCH = 7.32e6
+TRAFFIC_PER_LAUNCH = 4.55e6
 C6H6 = ("C 1.39 0 0; C 0.695 1.20377 0; C -0.695 1.20377 0; C -1.39 0 0; "
         "C -0.695 -1.20377 0; C 0.695 -1.20377 0; H 2.48 0 0; H 1.24 2.14774 0; "
         "H -1.24 2.14774 0; H -2.48 0 0; H -1.24 -2.14774 0; H 1.24 -2.14774 0")
