@@ -78,6 +78,8 @@ struct EPShape {
   int nslot;     // threads per walker in the electron phase (electron e on slot e % nslot)
   int nthreads;  // threads per block
   int ncol;      // W columns stored per AO (nmo_used rounded up to the MO chunk)
+  int pstride;   // split coordinates per walker row of the position arrays: 3 nelec made
+                 // odd, so that the 32 walkers of a warp read distinct banks
   int64_t smem;  // dynamic shared memory bytes
   int64_t o_tab, o_pos, o_pnew, o_mo, o_bk, o_jrow, o_vrow, o_dref, o_psi, o_f, o_kin, o_v,
       o_iel, o_acc;
@@ -100,10 +102,11 @@ __host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int 
   s.o_tab = o;
   o += tables_smem_bytes<R>(d, s.ncol);
   o = (o + 15) & ~int64_t(15);
+  s.pstride = (int)(nc | 1);
   s.o_pos = o;
-  o += align8(nwb * nc * xps);
+  o += align8(nwb * s.pstride * xps);
   s.o_pnew = o;
-  if (kind == 2) o += align8(nwb * nc * xps);
+  if (kind == 2) o += align8(nwb * s.pstride * xps);
   s.o_mo = o;
   o += align8(d.nelec * nmu * nwb * (int64_t)sizeof(R));
   s.o_bk = o;
@@ -503,7 +506,7 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   {
     const int slot = tid / nwb, wl = tid - (tid / nwb) * nwb;
     for (int e = slot; e < ne && slot < S.nslot; e += S.nslot)
-      ep_electron<R, JC, KIN>(d, t, pbuf + wl * nc, e, MO + wl, BK + wl, nwb, &JR[e * nwb + wl],
+      ep_electron<R, JC, KIN>(d, t, pbuf + wl * S.pstride, e, MO + wl, BK + wl, nwb, &JR[e * nwb + wl],
                               &VR[e * nwb + wl]);
   }
   __syncthreads();
@@ -541,16 +544,16 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
 }
 
 // Stage the positions of walkers [w0, w0 + nwb) into shared memory as split
-// coordinates; slots past the last walker repeat walker nw - 1 (a valid
-// configuration, never stored).
+// coordinates, rows of `ps` entries; slots past the last walker repeat walker
+// nw - 1 (a valid configuration, never stored).
 template <typename R>
 __device__ inline void ep_stage_positions(const double* pos, int64_t w0, int64_t nw, int nwb,
-                                          int nc, XP<R>* P) {
+                                          int nc, int ps, XP<R>* P) {
   for (int i = threadIdx.x; i < nwb * nc; i += blockDim.x) {
     const int wl = i / nc, c = i - wl * nc;
     int64_t w = w0 + wl;
     if (w >= nw) w = nw - 1;
-    P[i] = split_xp<R>(pos[w * nc + c]);
+    P[wl * ps + c] = split_xp<R>(pos[w * nc + c]);
   }
   __syncthreads();
 }

@@ -24,7 +24,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
                                                  unsigned char* smem) {
   const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
   const int64_t nw = a.nwalkers;
-  const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne;
+  const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne, ps = S.pstride;
   const int64_t w0 = block * nwb;
   const int tid = threadIdx.x;
   const int slot = tid / nwb, wl = tid - (tid / nwb) * nwb;
@@ -40,7 +40,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
   int* ACC = reinterpret_cast<int*>(smem + S.o_acc);
   const EPPtrs ptrs{smem, S};
   const double eps = 1e-16;
-  ep_stage_positions<R>(a.pos, w0, nw, nwb, nc, P);
+  ep_stage_positions<R>(a.pos, w0, nw, nwb, nc, ps, P);
   ep_eval<R, JC, false>(d, t, ptrs, P, scr, ss, w0, nw);
   int nacc = 0;
   double psi_cur = 0.0;  // combine threads: psi at the current positions
@@ -77,8 +77,8 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
       for (int e = slot; e < ne && active; e += nslot) {
         const bool moves = live && (a.move_type == QMC_MOVE_ALL_ELEC ||
                                     (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]));
-        XP<R>* pn = PN + wl * nc + 3 * e;
-        const XP<R>* pc = P + wl * nc + 3 * e;
+        XP<R>* pn = PN + wl * ps + 3 * e;
+        const XP<R>* pc = P + wl * ps + 3 * e;
         if (moves) {
           const double* rp =
               !a.proposals ? nullptr
@@ -117,7 +117,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
       __syncthreads();
       if (live && ACC[wl])
         for (int e = slot; e < ne; e += nslot)
-          for (int q = 0; q < 3; ++q) P[wl * nc + 3 * e + q] = PN[wl * nc + 3 * e + q];
+          for (int q = 0; q < 3; ++q) P[wl * ps + 3 * e + q] = PN[wl * ps + 3 * e + q];
       __syncthreads();
     }
     if (istep >= a.ntherm) {
@@ -125,7 +125,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
         if (a.samples && isnap < a.nsnap && live)
           for (int e = slot; e < ne; e += nslot) {
             double* out = a.samples + (isnap * nw + w) * nc + 3 * e;
-            for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * nc + 3 * e + q]);
+            for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * ps + 3 * e + q]);
           }
         ++isnap;
       }
@@ -134,7 +134,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
   }
   if (live)
     for (int e = slot; e < ne; e += nslot)
-      for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * nc + 3 * e + q]);
+      for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * ps + 3 * e + q]);
   if (tid < nwb && w0 + tid < nw) {
     if (a.accepted) a.accepted[w0 + tid] += nacc;
     if (a.psi_out) a.psi_out[w0 + tid] = psi_cur;
@@ -186,6 +186,7 @@ static int launch_metropolis_batch(const qmc_wf_desc* descs, const qmc_metropoli
   for (int j = 1; j < njobs; ++j) {
     const EPShape Sj = ep_shape<R>(descs[j], 2, S.nwb, JC, S.nslot);
     if (Sj.smem != S.smem || Sj.o_pos != S.o_pos || Sj.o_mo != S.o_mo || Sj.o_acc != S.o_acc ||
+        Sj.pstride != S.pstride ||
         Sj.ncol != S.ncol || Sj.nthreads != S.nthreads)
       return QMC_ERR_SHAPE;
   }

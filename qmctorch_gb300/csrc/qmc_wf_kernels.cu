@@ -21,7 +21,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_psi_kernel(const qmc_
   const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
   const int64_t w0 = (int64_t)blockIdx.x * S.nwb;
   XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);
-  ep_stage_positions<R>(pos, w0, nw, S.nwb, 3 * d.nelec, P);
+  ep_stage_positions<R>(pos, w0, nw, S.nwb, 3 * d.nelec, S.pstride, P);
   ep_eval<R, JC, false>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
   const int tid = threadIdx.x;
   if (tid < S.nwb && w0 + tid < nw)
@@ -39,7 +39,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_eloc_kernel(const qmc
   const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
   const int64_t w0 = (int64_t)blockIdx.x * S.nwb;
   XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);
-  ep_stage_positions<R>(pos, w0, nw, S.nwb, 3 * d.nelec, P);
+  ep_stage_positions<R>(pos, w0, nw, S.nwb, 3 * d.nelec, S.pstride, P);
   ep_eval<R, JC, true>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
   const int tid = threadIdx.x;
   if (tid < S.nwb && w0 + tid < nw) {
