@@ -68,7 +68,7 @@ def parse():
     p.add_argument("--serve-budget-gb", type=int, default=32)
     p.add_argument("--skip", default="",
                    help="comma list of sections to leave out (c6h6, serving, small, modules, "
-                        "precision, e2e); for short profiling runs")
+                        "mo_tc, precision, e2e); for short profiling runs")
     p.add_argument("--c6h6-sweeps", type=int, default=4,
                    help="all-elec-iter sweeps per timed C6H6 launch (mixed method)")
     p.add_argument("--mc-steps", type=int, default=100)
@@ -445,6 +445,54 @@ def bench_staged(torch, wf, x, flush):
     return out
 
 
+def bench_mo_tensor_core(torch, device, flush, nw_c6h6=16384, nw_h2o=16384):
+    """AO->MO of the module path (wf.mo(ao)) on the tensor cores
+    (qmc_mo_eval_tc, split-BF16 x3, FP32 accumulation) beside the FP64 kernel
+    (qmc_mo_eval): C6H6 cc-pVDZ (120 AOs -> 114 MOs) and H2O cc-pVDZ
+    (25 -> 24) at seeded positions, L2 flushed between timed calls. Reports
+    time per call, algorithmic HBM bytes (AO read + MO written, FP64) per
+    second against the copy peak, the BF16 tensor work the MMAs execute
+    (3 split products over the padded 128-row tiles) against the BF16 peak,
+    and the largest error relative to |AO| @ |W|."""
+    from qmctorch_gb300.scf import Molecule
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    peaks = {"hbm_gbs": 6800.0, "bf16_tflops": 1917.0}
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peaks.update({k: float(v) for k, v in json.load(f).items() if k in peaks})
+    except Exception:
+        pass
+    out = {"hbm_peak_gbs": peaks["hbm_gbs"], "bf16_peak_tflops": peaks["bf16_tflops"]}
+    for tag, geom, nw in (("c6h6_ccpvdz", C6H6, nw_c6h6), ("h2o_ccpvdz", H2O, nw_h2o)):
+        mol = Molecule(geom, unit="angs", basis="cc-pvdz")
+        wf64 = SlaterJastrow(mol, cuda=True, precision="fp64")
+        wfm = SlaterJastrow(mol, cuda=True, precision="mixed")
+        x = torch.as_tensor(seeded_positions(mol, nw, seed=11), device=device)
+        with torch.no_grad():
+            ao = wf64.ao(x)
+            rows, nao = nw * mol.nelec, ao.shape[-1]
+            ref = wf64.mo(ao)
+            got = wfm.mo(ao)
+            nmo = ref.shape[-1]
+            W = (wf64.mo.mo_scf * wf64.mo.mo_modifier).to(torch.float64)
+            scale = (ao.abs().reshape(rows, nao) @ W.abs()).reshape(ref.shape)
+            err = float(((got - ref).abs() / (scale + 1e-300)).max())
+            t_tc = _timed(torch, lambda i: wfm.mo(ao), 5, flush) / 5
+            t_64 = _timed(torch, lambda i: wf64.mo(ao), 3, flush) / 3
+        nbytes = rows * (nao + nmo) * 8
+        kp, npad = (nao + 15) // 16 * 16, (nmo + 15) // 16 * 16
+        tc_flops = 2.0 * ((rows + 127) // 128 * 128) * npad * 3 * kp
+        out[tag] = {"rows": rows, "nao": nao, "nmo": nmo, "ms_tc": t_tc * 1e3,
+                    "ms_fp64": t_64 * 1e3, "speedup_vs_fp64": t_64 / t_tc,
+                    "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / t_tc / 1e9,
+                    "frac_of_hbm": nbytes / t_tc / 1e9 / peaks["hbm_gbs"],
+                    "tensor_tflops": tc_flops / t_tc / 1e12,
+                    "frac_of_bf16": tc_flops / t_tc / 1e12 / peaks["bf16_tflops"],
+                    "max_err_rel_to_abs_product": err}
+        del ao, ref, got, scale
+    return out
+
+
 def bench_serving(args):
     """Continuous-batching single-point server on a seeded Poisson stream of
     H_n sto-3g requests (n even in 2..32, spacing 0.7-1.2 A, walkers
@@ -572,6 +620,8 @@ def run_gb300(args):
                                        and "serving" not in skip) else None)
     small = bench_h2_lih(torch, device) if rank == 0 and "small" not in skip else None
     staged = bench_staged(torch, wf64, x_eq, flush) if rank == 0 and "modules" not in skip else None
+    mo_tc = (bench_mo_tensor_core(torch, device, flush)
+             if rank == 0 and "mo_tc" not in skip else None)
 
     prec = (precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank))
             if rank == 0 and "precision" not in skip else None)
@@ -657,6 +707,7 @@ def run_gb300(args):
             "serving": serving,
             "small_configs": small,
             "module_kernels": staged,
+            "mo_tensor_core": mo_tc,
             "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }

@@ -55,7 +55,8 @@ enum qmc_status {
    sums and one iterative-refinement step of the solves that feed the kinetic
    energy in FP64; CI sums as FP32 ratios to the ground-state determinant
    scaled by its FP64 value. The staged module kernels
-   (qmc_ao_eval, qmc_mo_eval, qmc_jastrow_ee, qmc_slater) are FP64 always. */
+   (qmc_ao_eval, qmc_mo_eval, qmc_jastrow_ee, qmc_slater) are FP64 always;
+   qmc_mo_eval_tc is the mixed-precision (tensor-core) AO->MO module kernel. */
 #define QMC_PREC_FP64 0
 #define QMC_PREC_MIXED 1
 
@@ -176,6 +177,22 @@ int qmc_ao_eval(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, int32
  * Replaces MolecularOrbitals.forward (molecular_orbitals.py:79-95).
  */
 int qmc_mo_eval(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* mo, void* stream);
+
+/*
+ * qmc_mo_eval_tc: the same product mo[nrows][nmo] = ao[nrows][nao] @ W on the
+ * tensor cores (tcgen05.mma, FP32 accumulators in tensor memory), for the
+ * mixed-precision method. Split-BF16 x3: each FP64 operand is split into
+ * bf16 hi and lo parts and a_hi b_hi + a_hi b_lo + a_lo b_hi is accumulated
+ * in FP32, so |mo - ao @ W| <= about 2e-5 * (|ao| @ |W|) elementwise (the FP64
+ * qmc_mo_eval is exact to rounding). Replaces MolecularOrbitals.forward
+ * (molecular_orbitals.py:79-95) when the wave function runs in mixed
+ * precision. Limits: nmo <= 256 and shared memory for a 128 x 3 nao' tile of
+ * ao plus nmo' x 3 nao' of W in BF16 (nao', nmo' rounded up to 16; about
+ * nao <= 128 at nmo <= 128), else QMC_ERR_SHAPE. A tile whose tensor-core
+ * work does not complete within one second is written as NaN.
+ */
+int qmc_mo_eval_tc(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* mo,
+                   void* stream);
 
 /*
  * Pade e-e Jastrow. jast[nw] (J), djast[nw][3][ne] (gradient, sum_grad = 0) or

@@ -23,7 +23,7 @@ BUILD = os.path.join(ROOT, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
-           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu", "qmc_reduce.cu"]
+           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu", "qmc_reduce.cu", "qmc_mo_tc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 
@@ -123,6 +123,7 @@ SIGNATURES = {
     "qmc_ao_eval": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_int32, c_void_p, c_void_p,
                                    c_void_p, c_void_p]),
     "qmc_mo_eval": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
+    "qmc_mo_eval_tc": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_jastrow_ee": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                       c_void_p, c_int32, c_void_p]),
     "qmc_slater": (ctypes.c_int, [_P(WfDesc), c_void_p, c_void_p, c_int32, c_int64, c_void_p,

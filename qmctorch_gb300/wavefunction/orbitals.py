@@ -130,11 +130,17 @@ class AtomicOrbitals(nn.Module):
 
 
 class MolecularOrbitals(nn.Module):
-    """MO = AO @ (mo_scf * mo_modifier) (molecular_orbitals.py:7-95)."""
+    """MO = AO @ (mo_scf * mo_modifier) (molecular_orbitals.py:7-95).
+
+    ``precision`` (set by the owning wave function; default from torch's
+    default dtype as there) picks the kernel: "fp64" runs ``qmc_mo_eval``
+    (FP64, exact to rounding), "mixed" runs ``qmc_mo_eval_tc`` (tensor cores,
+    split-BF16 x3 with FP32 accumulation, error about 2e-5 of |AO| @ |W|)."""
 
     def __init__(self, mol, include_all_mo, highest_occ_mo, mix_mo, orthogonalize_mo, cuda):
         super().__init__()
         dtype = torch.get_default_dtype()
+        self.precision = "fp64" if dtype == torch.float64 else "mixed"
         self.mol = mol
         self.mix_mo = mix_mo
         self.orthogonalize_mo = orthogonalize_mo
@@ -171,6 +177,7 @@ class MolecularOrbitals(nn.Module):
             object.__setattr__(self, "_ao_module", AtomicOrbitals(self.mol))
         call = rt.build_desc(device, self._ao_module, mo=self)
         out = torch.empty((x.shape[0], self.mo_scf.shape[1]), dtype=rt.F64, device=device)
-        _lib.check(_lib.lib().qmc_mo_eval(call.ref, rt.ptr(x), x.shape[0], rt.ptr(out),
-                                          rt.stream_handle()), "qmc_mo_eval")
+        fn = "qmc_mo_eval_tc" if self.precision == "mixed" else "qmc_mo_eval"
+        _lib.check(getattr(_lib.lib(), fn)(call.ref, rt.ptr(x), x.shape[0], rt.ptr(out),
+                                           rt.stream_handle()), fn)
         return out.reshape(*ao.shape[:-1], -1).to(device=ao.device, dtype=ao.dtype)

@@ -152,6 +152,7 @@ class SlaterJastrow(WaveFunction):
         self.nmo_opt = mol.basis.nmo if include_all_mo else self.highest_occ_mo
         self.mo = MolecularOrbitals(mol, include_all_mo, self.highest_occ_mo, mix_mo,
                                     orthogonalize_mo, False)
+        self.mo.precision = precision
         self.pool = SlaterPooling(self.configs_method, self.configs, mol, False)
         self.fc = nn.Linear(self.nci, 1, bias=False)
         self.fc.weight.data.fill_(0.0)

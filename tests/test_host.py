@@ -196,3 +196,31 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu(name):
                                            gb, None) == 1  # ldw < nmo_used
     assert lib.qmc_wf_local_energy_adjoint(ctypes.byref(desc), v, 10, v, v, 1, v, v,
                                            desc.nmo_used, v, v, v, 8, None) == 3
+
+
+def test_tensor_core_mo_rejects_bad_arguments_and_shapes_without_a_gpu():
+    """qmc_mo_eval_tc checks arguments and its shape limits (nmo <= 256, the
+    split operand tiles within 227 KB of shared memory) before any device
+    call; an empty batch is a no-op."""
+    lib = _lib.lib()
+    desc, keep, wf = _desc_for("h2o_sd")
+    v = ctypes.c_void_p(8)
+    assert lib.qmc_mo_eval_tc(None, v, 10, v, None) == 1
+    assert lib.qmc_mo_eval_tc(ctypes.byref(desc), v, -1, v, None) == 1
+    assert lib.qmc_mo_eval_tc(ctypes.byref(desc), None, 10, v, None) == 1
+    assert lib.qmc_mo_eval_tc(ctypes.byref(desc), None, 0, None, None) == 0
+    desc.nmo = 300
+    assert lib.qmc_mo_eval_tc(ctypes.byref(desc), v, 10, v, None) == 2
+    desc.nmo, desc.nao = 128, 200
+    assert lib.qmc_mo_eval_tc(ctypes.byref(desc), v, 10, v, None) == 2
+    mol, d = load("h2")
+    old = torch.get_default_dtype()
+    try:
+        torch.set_default_dtype(torch.float32)
+        assert SlaterJastrow(mol).mo.precision == "mixed"
+        assert SlaterJastrow(mol, precision="fp64").mo.precision == "fp64"
+        torch.set_default_dtype(torch.float64)
+        assert SlaterJastrow(mol).mo.precision == "fp64"
+        assert SlaterJastrow(mol, precision="mixed").mo.precision == "mixed"
+    finally:
+        torch.set_default_dtype(old)
