@@ -68,7 +68,7 @@ def parse():
     p.add_argument("--serve-budget-gb", type=int, default=32)
     p.add_argument("--skip", default="",
                    help="comma list of sections to leave out (c6h6, serving, small, modules, "
-                        "mo_tc, precision, e2e); for short profiling runs")
+                        "mo_tc, h_n, precision, e2e); for short profiling runs")
     p.add_argument("--c6h6-sweeps", type=int, default=4,
                    help="all-elec-iter sweeps per timed C6H6 launch (mixed method)")
     p.add_argument("--mc-steps", type=int, default=100)
@@ -288,6 +288,28 @@ def metropolis_capi(torch, lib, wf, x, nstep, move_type, step, seed, generic=Fal
                                       ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)),
                "qmc_metropolis_run")
     return scratch, psi
+
+
+def bench_h_n(torch, lib, device, flush, nw=16384, nstep=50):
+    """Walker-steps/s of the mixed-method Metropolis kernel (all-electron moves,
+    step 0.2) on the serving workload's molecules: linear H_n sto-3g chains,
+    n = 2, 4, ..., 32 at 0.95 A spacing, single determinant + Pade e-e Jastrow,
+    16384 walkers, one launch of 50 steps per timed call."""
+    from qmctorch_gb300.scf import Molecule
+    from qmctorch_gb300.serving import hydrogen_chain
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    torch.set_default_dtype(torch.float64)
+    out = {"workload": "h_n_sto3g_ground_state_%dw_%d_steps" % (nw, nstep), "walker_steps_per_s": {}}
+    for n in range(2, 33, 2):
+        mol = Molecule(hydrogen_chain(n, 0.95), unit="angs", basis="sto-3g")
+        wf = SlaterJastrow(mol, cuda=True, precision="mixed")
+        x = torch.as_tensor(seeded_positions(mol, nw, seed=n), device=device)
+        scr, _ = metropolis_capi(torch, lib, wf, x, nstep, 0, STEP_SIZE, 5)
+        torch.cuda.synchronize()
+        t = _timed(torch, lambda i: metropolis_capi(torch, lib, wf, x, nstep, 0, STEP_SIZE, 6 + i,
+                                                    scratch=scr), 3, flush) / 3
+        out["walker_steps_per_s"]["H%d" % n] = nw * nstep / t
+    return out
 
 
 def bench_c6h6(torch, lib, args, device, flush, rank):
@@ -622,6 +644,7 @@ def run_gb300(args):
     staged = bench_staged(torch, wf64, x_eq, flush) if rank == 0 and "modules" not in skip else None
     mo_tc = (bench_mo_tensor_core(torch, device, flush)
              if rank == 0 and "mo_tc" not in skip else None)
+    h_n = bench_h_n(torch, lib, device, flush) if rank == 0 and "h_n" not in skip else None
 
     prec = (precision_study(torch, wf64, wfm, x_eq, sampler_for(777 + rank))
             if rank == 0 and "precision" not in skip else None)
@@ -708,6 +731,7 @@ def run_gb300(args):
             "small_configs": small,
             "module_kernels": staged,
             "mo_tensor_core": mo_tc,
+            "h_n_metropolis": h_n,
             "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }

@@ -138,8 +138,9 @@ int qmc_wf_psi(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double
  * QMC_STATIC_SCRATCH_BYTES array compiled into this library (every GPU that
  * loads the library keeps it for the life of the process). Limit: batches
  * whose qmc_scratch_bytes(d, nwalkers, 0) exceeds QMC_STATIC_SCRATCH_BYTES are
- * rejected with QMC_ERR_STATIC_LIMIT and nothing is launched (about 17,900
- * walkers of H2O cc-pVDZ with single_double(4,4)). The library allocates
+ * rejected with QMC_ERR_STATIC_LIMIT and nothing is launched (about 174,000
+ * walkers of H2O cc-pVDZ with single_double(4,4) in FP64: 96 bytes of
+ * determinant values per walker). The library allocates
  * nothing: no cudaMalloc, cudaFree or allocating library call.
  *
  * The first call on each device looks up the array's device address
@@ -186,10 +187,11 @@ int qmc_mo_eval(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* m
  * in FP32, so |mo - ao @ W| <= about 2e-5 * (|ao| @ |W|) elementwise (the FP64
  * qmc_mo_eval is exact to rounding). Replaces MolecularOrbitals.forward
  * (molecular_orbitals.py:79-95) when the wave function runs in mixed
- * precision. Limits: nmo <= 256 and shared memory for a 128 x 3 nao' tile of
- * ao plus nmo' x 3 nao' of W in BF16 (nao', nmo' rounded up to 16; about
- * nao <= 128 at nmo <= 128), else QMC_ERR_SHAPE. A tile whose tensor-core
- * work does not complete within one second is written as NaN.
+ * precision. Limits: nmo <= 256 and shared memory (227 KB) for two
+ * 128 x 2 nao' tiles of ao and one nmo' x 2 nao' tile of W in BF16 (nao', nmo'
+ * rounded up to 16; nao <= 128 at nmo <= 128 fits), else QMC_ERR_SHAPE. If a
+ * pipeline wait of the kernel runs out (1 s), the rows of the CTA concerned
+ * are written as NaN.
  */
 int qmc_mo_eval_tc(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* mo,
                    void* stream);

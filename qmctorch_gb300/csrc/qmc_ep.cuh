@@ -54,9 +54,12 @@ __host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
     o = align8(o);
   };
   const bool el = kind == 1;
+  // psi / Metropolis in excitation mode factor the Slater matrix in place in
+  // the block's shared-memory MO rows (ep_det): no LU or A^-1 A_virt arrays
+  const bool inplace = !el && d.det_mode == QMC_DET_EXCITATION;
   for (int s = 0; s < 2; ++s) {
-    add(L.lu[s], (int64_t)nmax * nmax, rsz);
-    add(L.x[s], (int64_t)nmax * vmax, rsz);
+    add(L.lu[s], inplace ? 0 : (int64_t)nmax * nmax, rsz);
+    add(L.x[s], inplace ? 0 : (int64_t)nmax * vmax, rsz);
     add(L.y[s], el ? (int64_t)nmax * omax : 0, rsz);
     add(L.x64[s], (el && mixed) ? (int64_t)nmax * vmax : 0, 8);
     add(L.y64[s], (el && mixed) ? (int64_t)nmax * omax : 0, 8);
@@ -459,7 +462,7 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
 // ---------------------------------------------------------------------------
 template <typename R, bool OP>
 __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned char* scr,
-                              int64_t ss, int64_t w, int spin, const R* mo_s, const R* bk_s, int wl,
+                              int64_t ss, int64_t w, int spin, R* mo_s, const R* bk_s, int wl,
                               int nwb, double* dref) {
   using T = typename std::conditional<OP, double, R>::type;
   const int row0 = spin ? d.nup : 0;
@@ -474,6 +477,15 @@ __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned 
   wk.rc = MView<R>{rptr<R>(scr, L.rc[spin], ss, w), ss, ss};
   wk.X64 = MView<double>{rptr<double>(scr, L.x64[spin], ss, w), vm * ss, ss};
   wk.Y64 = MView<double>{rptr<double>(scr, L.y64[spin], ss, w), (int64_t)L.omax * ss, ss};
+  if (!OP && d.det_mode == QMC_DET_EXCITATION) {
+    // in place (the MO rows are recomputed before every evaluation): the LU of
+    // the occupied columns and A^-1 A_virt over the virtual columns of the
+    // spin's MO rows, the same operations in the same order as on copies
+    R* rows = mo_s + row0 * rs + wl;
+    const int n = spin ? d.ndown : d.nup;
+    wk.LU = MView<R>{rows, rs, cs};
+    wk.X = MView<R>{rows + n * cs, rs, cs};
+  }
   T* dv = rptr<T>(scr, L.dv, ss, w) + (spin ? d.ndet[0] * ss : 0);
   double* ov = OP ? rptr<double>(scr, L.ov, ss, w) + (spin ? d.ndet[0] * ss : 0) : nullptr;
   spin_channel<R, OP, T>(d, spin, mo, bk, wk, SpinOut<T>{dv, ov, ss, &dref[spin * nwb + wl]});

@@ -113,8 +113,14 @@ static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, 
   const int kmax = (kind == 1 && !kMixed<R>) ? 1 : 8;
   EPShape best = s1;
   best.smem = -1;  // nothing fits yet
-  for (; nwb >= 1 && best.smem < 0; nwb /= 2) {
-    double best_fill = -1.0;
+  double best_fill = -1.0;
+  bool one_wave = false;
+  for (; nwb >= 1 && !one_wave; nwb /= 2) {
+    // the first block size that fits is kept, except by the persistent
+    // Metropolis kernel (kind 2), which halves it down to 8 walkers while no
+    // thread split gives a single wave (a partial last wave would run alone
+    // for all the launch's steps); a smaller size must fill strictly better
+    if (best.smem >= 0 && (kind != 2 || nwb < 8)) break;
     for (int k = 1; k <= kmax; ++k) {
       const int nslot = (ne + k - 1) / k;
       if (k > 1 && nslot == (ne + k - 2) / (k - 1)) continue;  // same slot count as k - 1
@@ -131,6 +137,7 @@ static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, 
       const int64_t blocks = (nw + nwb - 1) / nwb, slots = (int64_t)occ * nsm;
       if (blocks <= slots) {  // one wave
         best = s;
+        one_wave = true;
         break;
       }
       const double fill = (double)blocks / (double)(((blocks + slots - 1) / slots) * slots);

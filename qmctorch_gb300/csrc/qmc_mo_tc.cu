@@ -4,23 +4,33 @@
 //
 // Split-BF16 x3 with FP32 accumulation. Every FP64 operand x is split into
 // x_hi = bf16(x) and x_lo = bf16(x - x_hi) (x_hi + x_lo holds ~16 significant
-// bits). The three products a_hi b_hi + a_hi b_lo + a_lo b_hi are one BF16 GEMM
-// of depth 3 K over the concatenated operands
-//     A' = [a_hi | a_hi | a_lo],   B' = [b_hi | b_lo | b_hi],
-// so a single chain of tcgen05.mma instructions accumulates all of them in
-// TMEM. Error per output: about 2^-16 of sum_k |a_k| |b_k| (the dropped
-// a_lo b_lo term and the split residuals), plus FP32 accumulation rounding.
+// bits). The three products a_hi b_hi + a_hi b_lo + a_lo b_hi form one chain
+// of tcgen05.mma instructions of depth 3 K accumulated in TMEM: shared memory
+// holds each operand once as [hi | lo] and the MMA descriptors of the three
+// K segments point at (a_hi, b_hi), (a_hi, b_lo), (a_lo, b_hi). Error per
+// output: about 2^-16 of sum_k |a_k| |b_k| (the dropped a_lo b_lo term and the
+// split residuals), plus FP32 accumulation rounding.
 //
-// Tiles: one CTA per 128 AO rows at a time (M = 128 = TMEM lanes), persistent
-// over row tiles. B' (N x 3K, N = nmo rounded up to 16) is built once per CTA
-// in shared memory; the A' tile is staged by all threads (FP64 loads, split,
-// 16-byte shared stores) in the canonical K-major no-swizzle layout of the
-// tensor core: 8 x 16-byte core matrices, adjacent along K 128 bytes apart
-// (leading byte offset), adjacent 8-row groups 3K * 16 bytes apart (stride
-// byte offset). One elected thread issues the 3K / 16 MMAs (128 x N x 16
-// each) and commits them to an mbarrier; the eight warps then read the FP32
-// accumulators back with tcgen05.ld (warp w: lanes 32 (w % 4) .. + 31, column
-// chunks of 16 alternating between the two warpgroups) and store FP64.
+// Operand layout: canonical K-major, no swizzle: 8-row x 16-byte core
+// matrices, adjacent along K 128 bytes apart (leading byte offset), adjacent
+// 8-row groups 2 K' * 16 bytes apart (stride byte offset; K' = nao rounded up
+// to 16).
+//
+// Warp-specialised persistent CTA (17 warps), one 128-row tile of AO rows at
+// a time (M = 128 = TMEM lanes):
+//   warps 0-7   producers: FP64 AO rows -> split -> 16-byte shared stores into
+//               one of two A buffers;
+//   warp 8      allocates TMEM; lane 0 issues the MMA chain of a tile into one
+//               of two TMEM accumulators and commits it to two mbarriers
+//               (A buffer free, accumulator full);
+//   warps 9-16  epilogue: tcgen05.ld of the accumulator (warp w reads TMEM
+//               lanes 32 (w % 4) .. + 31; the two groups of four alternate
+//               16-column chunks) and FP64 stores of the MO rows.
+// So the loads of tile i + 1, the MMAs of tile i and the stores of tile i - 1
+// overlap. Every mbarrier wait is bounded (1 s); on a timeout the CTA raises
+// a shared abort flag, all roles leave their loops, the CTA's tiles are
+// written as NaN, and TMEM is released after a bounded wait for the tensor
+// core.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -30,37 +40,49 @@
 namespace qmc {
 namespace tc {
 
-constexpr int kM = 128;          // rows per tile (TMEM lanes, MMA M)
-constexpr int kThreads = 256;    // 8 warps: two warpgroups share the epilogue columns
-constexpr int kMaxN = 256;       // MMA N limit for M = 128
+constexpr int kM = 128;                 // rows per tile (TMEM lanes, MMA M)
+constexpr int kProducerWarps = 8;
+constexpr int kMmaWarp = kProducerWarps;  // warp 8
+constexpr int kEpilogueWarps = 8;
+constexpr int kWarps = kProducerWarps + 1 + kEpilogueWarps;
+constexpr int kThreads = kWarps * 32;   // 544
+constexpr int kProducerThreads = kProducerWarps * 32;
+constexpr int kEpilogueThreads = kEpilogueWarps * 32;
+constexpr int kMaxN = 256;              // MMA N limit for M = 128
 constexpr uint64_t kWaitNs = 1000000000ull;  // mbarrier wait limit: 1 s
 
 struct Shape {
   int kp;        // K of one piece (nao rounded up to 16)
-  int kk;        // GEMM depth 3 kp
+  int kc;        // stored depth 2 kp ([hi | lo])
   int n;         // MMA N (nmo rounded up to 16)
-  int tmem_cols; // power of two >= max(32, n)
-  int64_t a_off, b_off, bar_off, smem;
+  int acc_cols;  // TMEM columns of one accumulator: power of two >= max(32, n)
+  int64_t a_off[2], b_off, bar_off, smem;
 };
+
+// barriers at bar_off: full[2], empty[2], dfull[2], dempty[2] (8 B each), then
+// the TMEM address (4 B) and the abort flag (4 B)
+constexpr int kBarFull = 0, kBarEmpty = 2, kBarDFull = 4, kBarDEmpty = 6, kNumBars = 8;
 
 __host__ __device__ inline Shape shape(int nao, int nmo) {
   Shape s;
   s.kp = (nao + 15) & ~15;
-  s.kk = 3 * s.kp;
+  s.kc = 2 * s.kp;
   s.n = (nmo + 15) & ~15;
-  s.tmem_cols = 32;
-  while (s.tmem_cols < s.n) s.tmem_cols *= 2;
-  s.a_off = 0;
-  s.b_off = s.a_off + (int64_t)kM * s.kk * 2;
-  s.bar_off = s.b_off + (int64_t)s.n * s.kk * 2;
-  s.smem = s.bar_off + 16 + 1024;  // mbarrier (8 B), TMEM address (4 B); 1 KB for base alignment
+  s.acc_cols = 32;
+  while (s.acc_cols < s.n) s.acc_cols *= 2;
+  const int64_t a_bytes = (int64_t)kM * s.kc * 2;
+  s.a_off[0] = 0;
+  s.a_off[1] = a_bytes;
+  s.b_off = 2 * a_bytes;
+  s.bar_off = s.b_off + (int64_t)s.n * s.kc * 2;
+  s.smem = s.bar_off + kNumBars * 8 + 8 + 1024;  // 1 KB for base alignment
   return s;
 }
 
 // Byte offset of the 16-byte chunk holding elements (r, 8 c .. 8 c + 7) of a
-// K-major operand with depth kk in the no-swizzle canonical layout.
-__host__ __device__ inline uint32_t chunk_offset(int r, int c, int kk) {
-  return (uint32_t)((r >> 3) * (kk * 16) + c * 128 + (r & 7) * 16);
+// K-major operand of stored depth kc in the no-swizzle canonical layout.
+__host__ __device__ inline uint32_t chunk_offset(int r, int c, int kc) {
+  return (uint32_t)((r >> 3) * (kc * 16) + c * 128 + (r & 7) * 16);
 }
 
 // Shared-memory matrix descriptor (tcgen05): start address, leading byte
@@ -85,8 +107,9 @@ __device__ inline uint64_t global_ns() {
 }
 
 // Bounded wait for the completion of phase `parity` of the mbarrier at
-// shared address `bar`; false after kWaitNs.
-__device__ inline bool mbar_wait(uint32_t bar, uint32_t parity) {
+// shared address `bar`. Returns false after kWaitNs or when another thread
+// raised the abort flag (and then raises it itself).
+__device__ inline bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
   const uint64_t t0 = global_ns();
   while (true) {
     uint32_t done;
@@ -97,8 +120,22 @@ __device__ inline bool mbar_wait(uint32_t bar, uint32_t parity) {
         : "r"(bar), "r"(parity)
         : "memory");
     if (done) return true;
-    if (global_ns() - t0 > kWaitNs) return false;
+    if (*abort_flag) return false;
+    if (global_ns() - t0 > kWaitNs) {
+      *abort_flag = 1;
+      return false;
+    }
   }
+}
+
+__device__ inline void mbar_arrive(uint32_t bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(bar) : "memory");
+}
+
+__device__ inline void mma_commit(uint32_t bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(bar)
+      : "memory");
 }
 
 __device__ inline uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
@@ -146,11 +183,43 @@ __device__ inline void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
 }
 
-__global__ void __launch_bounds__(kThreads) mo_tc_kernel(const double* __restrict__ ao,
-                                                         int64_t nrows, int nao, int nmo,
-                                                         const double* __restrict__ mo_scf,
-                                                         const double* __restrict__ mo_mod,
-                                                         double* __restrict__ mo) {
+// FP64 values (row, 8 c .. 8 c + 7) of a row-major [nrows][nao] array, zero
+// outside it; 16-byte loads when the chunk is 16-byte aligned.
+__device__ inline void load8(const double* __restrict__ ao, int64_t row, int64_t nrows, int nao,
+                             int c, double (&v)[8]) {
+  const int k0 = c * 8;
+  if (row < nrows && k0 + 8 <= nao) {
+    const double* src = ao + row * nao + k0;
+    if ((reinterpret_cast<uintptr_t>(src) & 15) == 0) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const double2 t = __ldg(reinterpret_cast<const double2*>(src) + j);
+        v[2 * j] = t.x;
+        v[2 * j + 1] = t.y;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) v[j] = __ldg(src + j);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 8; ++j)
+      v[j] = (row < nrows && k0 + j < nao) ? __ldg(ao + row * nao + k0 + j) : 0.0;
+  }
+}
+
+// Bounded wait used once, at exit after an abort, for the tensor core to
+// finish the last committed MMA chain before TMEM is released.
+__device__ inline void mbar_wait_final(uint32_t bar, uint32_t parity) {
+  volatile int never = 0;
+  mbar_wait(bar, parity, &never);
+}
+
+__global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __restrict__ ao,
+                                                            int64_t nrows, int nao, int nmo,
+                                                            const double* __restrict__ mo_scf,
+                                                            const double* __restrict__ mo_mod,
+                                                            double* __restrict__ mo, int vec) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const Shape S = shape(nao, nmo);
   // 1 KB-aligned base (the dynamic shared-memory window is only 16-byte aligned)
@@ -158,25 +227,34 @@ __global__ void __launch_bounds__(kThreads) mo_tc_kernel(const double* __restric
   const uint32_t pad = (1024u - (raw_addr & 1023u)) & 1023u;
   unsigned char* smem = smem_raw + pad;
   const uint32_t base = raw_addr + pad;
-  const uint32_t a_addr = base + (uint32_t)S.a_off, b_addr = base + (uint32_t)S.b_off;
-  const uint32_t bar = base + (uint32_t)S.bar_off;
-  volatile uint32_t* tmem_slot = reinterpret_cast<volatile uint32_t*>(smem + S.bar_off + 8);
+  const uint32_t b_addr = base + (uint32_t)S.b_off;
+  const uint32_t bars = base + (uint32_t)S.bar_off;  // mbarrier k at bars + 8 k
+  const uint32_t tmem_slot_addr = bars + kNumBars * 8;
+  volatile uint32_t* tmem_slot =
+      reinterpret_cast<volatile uint32_t*>(smem + S.bar_off + kNumBars * 8);
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(smem + S.bar_off + kNumBars * 8 + 4);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int cpk = S.kp >> 3;  // 16-byte chunks per piece and row
+  const int64_t ntiles = (nrows + kM - 1) / kM;
 
-  // -- set-up: TMEM columns (warp 0), the mbarrier, B' in shared memory ------
-  if (warp == 0) {
+  // -- set-up: two TMEM accumulators (warp 8), mbarriers, B = [W_hi | W_lo] -
+  if (warp == kMmaWarp) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(
-                     base + (uint32_t)S.bar_off + 8),
-                 "r"((uint32_t)S.tmem_cols)
+                     tmem_slot_addr),
+                 "r"((uint32_t)(2 * S.acc_cols))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
   }
   if (tid == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(bar) : "memory");
+    const uint32_t counts[kNumBars] = {kProducerThreads, kProducerThreads, 1, 1, 1, 1,
+                                       kEpilogueThreads, kEpilogueThreads};
+    for (int k = 0; k < kNumBars; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(bars + 8 * k),
+                   "r"(counts[k])
+                   : "memory");
+    *abort_flag = 0;
     asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
   }
-  // B'[n][k]: W[k][n] split; pieces [hi | lo | hi]; zero past nao / nmo
   for (int i = tid; i < S.n * cpk; i += kThreads) {
     const int nr = i & 7, c = (i >> 3) % cpk, ng = (i >> 3) / cpk;
     const int n = ng * 8 + nr;
@@ -190,9 +268,8 @@ __global__ void __launch_bounds__(kThreads) mo_tc_kernel(const double* __restric
     }
     uint4 hi, lo;
     split8(v, hi, lo);
-    *reinterpret_cast<uint4*>(smem + S.b_off + chunk_offset(n, c, S.kk)) = hi;
-    *reinterpret_cast<uint4*>(smem + S.b_off + chunk_offset(n, cpk + c, S.kk)) = lo;
-    *reinterpret_cast<uint4*>(smem + S.b_off + chunk_offset(n, 2 * cpk + c, S.kk)) = hi;
+    *reinterpret_cast<uint4*>(smem + S.b_off + chunk_offset(n, c, S.kc)) = hi;
+    *reinterpret_cast<uint4*>(smem + S.b_off + chunk_offset(n, cpk + c, S.kc)) = lo;
   }
   fence_proxy_async();
   fence_before_sync();
@@ -200,84 +277,128 @@ __global__ void __launch_bounds__(kThreads) mo_tc_kernel(const double* __restric
   fence_after_sync();
   const uint32_t tmem = *tmem_slot;
 
-  const uint32_t idesc = instr_desc(kM, S.n);
-  const uint32_t lbo = 128, sbo = (uint32_t)S.kk * 16;
-  const int nsteps = S.kk / 16;
-  const int64_t ntiles = (nrows + kM - 1) / kM;
-  const int q = warp & 3, half = warp >> 2;
-  const int nchunk = S.n / 16;
-  uint32_t phase = 0;
-
-  for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int64_t row0 = tile * kM;
-    // -- stage A' = [hi | hi | lo] of rows row0 .. row0 + 127 ---------------
-    for (int i = tid; i < kM * cpk; i += kThreads) {
-      const int rr = i & 7, c = (i >> 3) % cpk, rg = (i >> 3) / cpk;
-      const int r = rg * 8 + rr;
-      const int64_t row = row0 + r;
-      double v[8];
-      const double* src = ao + row * nao + c * 8;
+  int last = -1;  // MMA thread: index of the last tile whose chain was committed
+  if (warp < kProducerWarps) {
+    // -- producers: AO rows of tile i -> [hi | lo] into A buffer i % 2 ------
+    const int nitems = kM * cpk;
+    int i = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const int b = i & 1, use = i >> 1;
+      if (use > 0 && !mbar_wait(bars + 8 * (kBarEmpty + b), (uint32_t)((use - 1) & 1), abort_flag))
+        break;
+      const int64_t row0 = tile * kM;
+      unsigned char* A = smem + S.a_off[b];
+      for (int it = tid; it < nitems; it += 2 * kProducerThreads) {
+        const int it1 = it + kProducerThreads;
+        const bool two = it1 < nitems;
+        double v0[8], v1[8];
+        const int r0 = ((it >> 3) / cpk) * 8 + (it & 7), c0 = (it >> 3) % cpk;
+        const int r1 = ((it1 >> 3) / cpk) * 8 + (it1 & 7), c1 = (it1 >> 3) % cpk;
+        load8(ao, row0 + r0, nrows, nao, c0, v0);
+        if (two) load8(ao, row0 + r1, nrows, nao, c1, v1);
+        uint4 hi, lo;
+        split8(v0, hi, lo);
+        *reinterpret_cast<uint4*>(A + chunk_offset(r0, c0, S.kc)) = hi;
+        *reinterpret_cast<uint4*>(A + chunk_offset(r0, cpk + c0, S.kc)) = lo;
+        if (two) {
+          split8(v1, hi, lo);
+          *reinterpret_cast<uint4*>(A + chunk_offset(r1, c1, S.kc)) = hi;
+          *reinterpret_cast<uint4*>(A + chunk_offset(r1, cpk + c1, S.kc)) = lo;
+        }
+      }
+      fence_proxy_async();
+      mbar_arrive(bars + 8 * (kBarFull + b));
+    }
+  } else if (warp == kMmaWarp) {
+    // -- one thread issues the MMA chain of tile i into accumulator i % 2 ---
+    if (lane == 0) {
+      const uint32_t idesc = instr_desc(kM, S.n);
+      const uint32_t lbo = 128, sbo = (uint32_t)S.kc * 16;
+      const int spp = S.kp / 16;  // MMA steps per K segment
+      int i = 0;
+      for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        const int b = i & 1, use = i >> 1;
+        if (!mbar_wait(bars + 8 * (kBarFull + b), (uint32_t)(use & 1), abort_flag)) break;
+        if (use > 0 &&
+            !mbar_wait(bars + 8 * (kBarDEmpty + b), (uint32_t)((use - 1) & 1), abort_flag))
+          break;
+        fence_after_sync();
+        const uint32_t dt = tmem + (uint32_t)(b * S.acc_cols);
+        const uint32_t a_base = base + (uint32_t)S.a_off[b];
+        for (int s = 0; s < 3 * spp; ++s) {
+          const int seg = s / spp, sub = s - seg * spp;
+          // segments: (a_hi, b_hi), (a_hi, b_lo), (a_lo, b_hi)
+          const int ap = seg == 2 ? 1 : 0, bp = seg == 1 ? 1 : 0;
+          const uint64_t ad = smem_desc(a_base + (uint32_t)((ap * cpk + 2 * sub) * 128), lbo, sbo);
+          const uint64_t bd = smem_desc(b_addr + (uint32_t)((bp * cpk + 2 * sub) * 128), lbo, sbo);
+          const uint32_t acc = s > 0 ? 1u : 0u;
+          asm volatile(
+              "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
+              " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(dt),
+              "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
+              : "memory");
+        }
+        mma_commit(bars + 8 * (kBarEmpty + b));
+        mma_commit(bars + 8 * (kBarDFull + b));
+        last = i;
+      }
+    }
+    __syncwarp();
+  } else {
+    // -- epilogue: accumulator i % 2 -> registers -> FP64 rows --------------
+    const int q = warp & 3, half = (warp - kMmaWarp - 1) >> 2;
+    const int nchunk = S.n / 16;
+    int i = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const int d = i & 1, use = i >> 1;
+      bool ok = mbar_wait(bars + 8 * (kBarDFull + d), (uint32_t)(use & 1), abort_flag);
+      ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below needs the whole warp
+      if (!ok) break;
+      fence_after_sync();
+      const uint32_t dt = tmem + (uint32_t)(d * S.acc_cols) + ((uint32_t)(q * 32) << 16);
+      const int64_t row = tile * kM + q * 32 + lane;
+      for (int ch = half; ch < nchunk; ch += 2) {
+        float v[16];
+        tmem_ld16(dt + (uint32_t)(ch * 16), v);
+        if (row < nrows) {
+          double* dst = mo + row * nmo + ch * 16;
+          if (vec) {
 #pragma unroll
-      for (int j = 0; j < 8; ++j) v[j] = (row < nrows && c * 8 + j < nao) ? __ldg(src + j) : 0.0;
-      uint4 hi, lo;
-      split8(v, hi, lo);
-      *reinterpret_cast<uint4*>(smem + S.a_off + chunk_offset(r, c, S.kk)) = hi;
-      *reinterpret_cast<uint4*>(smem + S.a_off + chunk_offset(r, cpk + c, S.kk)) = hi;
-      *reinterpret_cast<uint4*>(smem + S.a_off + chunk_offset(r, 2 * cpk + c, S.kk)) = lo;
-    }
-    fence_proxy_async();
-    fence_before_sync();  // the previous tile's tcgen05.ld before the next MMA
-    __syncthreads();
-    fence_after_sync();
-    // -- one thread issues the MMA chain and commits it to the mbarrier ----
-    if (tid == 0) {
-      for (int s = 0; s < nsteps; ++s) {
-        const uint64_t ad = smem_desc(a_addr + (uint32_t)s * 256u, lbo, sbo);
-        const uint64_t bd = smem_desc(b_addr + (uint32_t)s * 256u, lbo, sbo);
-        const uint32_t acc = s > 0 ? 1u : 0u;
-        asm volatile(
-            "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n"
-            " tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(tmem),
-            "l"(ad), "l"(bd), "r"(idesc), "r"(acc)
-            : "memory");
-      }
-      asm volatile(
-          "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(
-              bar)
-          : "memory");
-    }
-    const bool ok = mbar_wait(bar, phase);
-    phase ^= 1u;
-    if (__syncthreads_or(!ok)) {
-      // the MMAs did not complete within the limit: mark this tile's rows
-      // NaN, give the tensor core a second bounded wait, release TMEM, stop
-      for (int i = tid; i < kM * nmo; i += kThreads) {
-        const int64_t row = row0 + i / nmo;
-        if (row < nrows) mo[row * nmo + i % nmo] = __longlong_as_double(0x7ff8000000000000ll);
-      }
-      if (!ok) mbar_wait(bar, phase ^ 1u);
-      break;
-    }
-    fence_after_sync();
-    // -- epilogue: TMEM -> registers -> FP64 rows --------------------------
-    const int64_t row = row0 + q * 32 + lane;
-    for (int ch = half; ch < nchunk; ch += 2) {
-      float v[16];
-      tmem_ld16(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(ch * 16), v);
-      if (row < nrows) {
-        double* dst = mo + row * nmo + ch * 16;
+            for (int j = 0; j < 8; ++j)
+              if (ch * 16 + 2 * j < nmo)
+                reinterpret_cast<double2*>(dst)[j] = make_double2((double)v[2 * j],
+                                                                  (double)v[2 * j + 1]);
+          } else {
 #pragma unroll
-        for (int j = 0; j < 16; ++j)
-          if (ch * 16 + j < nmo) dst[j] = (double)v[j];
+            for (int j = 0; j < 16; ++j)
+              if (ch * 16 + j < nmo) dst[j] = (double)v[j];
+          }
+        }
       }
+      fence_before_sync();
+      mbar_arrive(bars + 8 * (kBarDEmpty + d));
     }
   }
+
   fence_before_sync();
   __syncthreads();
   fence_after_sync();
-  if (warp == 0)
+  if (*abort_flag) {
+    // a wait ran out: this CTA's rows are written as NaN, and the tensor core
+    // gets a bounded wait for its last committed chain before TMEM is freed
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
+      for (int idx = tid; idx < kM * nmo; idx += kThreads) {
+        const int64_t row = tile * kM + idx / nmo;
+        if (row < nrows) mo[row * nmo + idx % nmo] = __longlong_as_double(0x7ff8000000000000ll);
+      }
+    if (last >= 0) mbar_wait_final(bars + 8 * (kBarDFull + (last & 1)), (uint32_t)((last >> 1) & 1));
+    fence_before_sync();
+    __syncthreads();
+    fence_after_sync();
+  }
+  if (warp == kMmaWarp)
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem),
-                 "r"((uint32_t)S.tmem_cols)
+                 "r"((uint32_t)(2 * S.acc_cols))
                  : "memory");
 }
 
@@ -309,12 +430,13 @@ int qmc_mo_eval_tc(const qmc_wf_desc* d, const double* ao, int64_t nrows, double
   }
   // resident CTAs of one SM must fit its 512 TMEM columns together, so that
   // no tcgen05.alloc waits on another CTA
-  if (occ > 512 / S.tmem_cols) occ = 512 / S.tmem_cols;
+  if (occ > 512 / (2 * S.acc_cols)) occ = 512 / (2 * S.acc_cols);
   const int64_t ntiles = (nrows + tc::kM - 1) / tc::kM;
   int64_t grid = (int64_t)nsm * occ;
   if (grid > ntiles) grid = ntiles;
+  const int vec = (d->nmo % 2 == 0) && ((reinterpret_cast<uintptr_t>(mo) & 15) == 0);
   tc::mo_tc_kernel<<<(unsigned)grid, tc::kThreads, S.smem, (cudaStream_t)stream>>>(
-      ao, nrows, d->nao, d->nmo, d->mo_scf, d->mo_modifier, mo);
+      ao, nrows, d->nao, d->nmo, d->mo_scf, d->mo_modifier, mo, vec);
   return launch_status();
 }
 
