@@ -12,7 +12,9 @@ reference outputs: AO values and derivatives, MOs, Jastrow factor and
 derivatives, Slater determinants, psi, pdf, their electron-position
 gradients (gradients_jacobi), kinetic and local energies, a
 Metropolis replay with injected proposals and uniforms, and the parameter
-gradients of the manual and automatic VMC energy gradients.
+gradients of the manual and automatic VMC energy gradients. ``gmetropolis``
+writes ``tests/golden/gmetropolis.npz``: chains of the reference's
+GeneralizedMetropolis (drift-diffusion) sampler on an analytic density.
 """
 import os
 import sys
@@ -206,5 +208,52 @@ def main(reference_root, only=()):
         print("wrote", out_file, os.path.getsize(out_file), "bytes")
 
 
+# Drift-diffusion (generalized Metropolis) chains of the reference sampler on
+# an analytic density: rho(x) = exp(-sum_k a_k (x_k - c_k)^2) over the flattened
+# walker coordinates, drift by the reference's own autograd (get_drift).
+GMET = {"nwalkers": 24, "nelec": 2, "ndim": 3, "nstep": 30, "step_size": 0.3,
+        "ntherm": -10, "ndecor": 2, "seed": 2024}
+
+
+def gmet_density_params():
+    rng = np.random.default_rng(5)
+    n = GMET["nelec"] * GMET["ndim"]
+    return rng.uniform(0.4, 1.6, size=n), rng.uniform(-0.5, 0.5, size=n)
+
+
+def make_gmetropolis(reference_root):
+    ref_stubs.install(reference_root)
+    import torch
+    from qmctorch.sampler.generalized_metropolis import GeneralizedMetropolis
+    from qmctorch.utils import set_torch_double_precision
+
+    set_torch_double_precision()
+    a, c = gmet_density_params()
+    at, ct = torch.as_tensor(a), torch.as_tensor(c)
+
+    def pdf(x):
+        return torch.exp(-(at * (x - ct) ** 2).sum(-1))
+
+    pos0 = np.random.default_rng(6).normal(size=(GMET["nwalkers"], GMET["nelec"] * GMET["ndim"]))
+    g = GMET
+    sampler = GeneralizedMetropolis(nwalkers=g["nwalkers"], nstep=g["nstep"],
+                                    step_size=g["step_size"], ntherm=g["ntherm"],
+                                    ndecor=g["ndecor"], nelec=g["nelec"], ndim=g["ndim"],
+                                    init={"method": "uniform", "min": -1, "max": 1})
+    torch.manual_seed(g["seed"])
+    samples = sampler(pdf, pos=torch.as_tensor(pos0), with_tqdm=False)
+    out_file = os.path.join(HERE, "gmetropolis.npz")
+    np.savez_compressed(out_file, a=a, c=c, pos0=pos0, samples=samples.detach().numpy(),
+                        final=sampler.walkers.pos.detach().numpy(),
+                        **{"cfg_" + k: np.asarray(v) for k, v in GMET.items()})
+    print("wrote", out_file, os.path.getsize(out_file), "bytes")
+
+
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference", tuple(sys.argv[2:]))
+    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    names = tuple(sys.argv[2:])
+    if "gmetropolis" in names or not names:
+        make_gmetropolis(root)
+    names = tuple(n for n in names if n != "gmetropolis")
+    if names or len(sys.argv) <= 2:
+        main(root, names)
