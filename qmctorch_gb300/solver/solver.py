@@ -137,6 +137,36 @@ class SolverBase:
         log.info("  Size     : %d", len(eloc))
         return SimpleNamespace(pos=pos, local_energy=eloc, energy=e, variance=s, error=err)
 
+    def sampling_traj(self, pos=None, with_tqdm=True, hdf5_group="sampling_trajectory"):
+        """Local energies along a sampling trajectory (solver_base.py:435-471):
+        ``local_energy`` of shape (nsnapshots, nwalkers) as a numpy array and
+        the positions. The snapshots are evaluated in one fused local-energy
+        call instead of one call per snapshot."""
+        log.info("  Sampling trajectory")
+        with torch.no_grad():
+            if pos is None:
+                pos = self.sampler(self.wf.pdf, with_tqdm=with_tqdm)
+            nw = self.sampler.walkers.nwalkers
+            flat = pos.detach().reshape(-1, pos.shape[-1])
+            if self.wf.cuda and flat.device.type == "cpu":
+                flat = flat.to(self.device)
+            el = self.wf.local_energy(flat).reshape(-1, nw).cpu().numpy()
+        return SimpleNamespace(local_energy=el, pos=pos)
+
+    def print_parameters(self, grad=False):
+        """Print the trainable parameters, or their gradients (solver_base.py:473-484)."""
+        for p in self.wf.parameters():
+            if p.requires_grad:
+                print(p.grad if grad else p)
+
+    def optimization_step(self, lpos):
+        """One optimiser step; optimisers that need the positions get them
+        (solver_base.py:486-496)."""
+        if getattr(self.opt, "lpos_needed", False):
+            self.opt.step(lpos)
+        else:
+            self.opt.step()
+
     def save_checkpoint(self, epoch, loss):
         filename = "checkpoint_epoch%d.pth" % epoch
         torch.save({"epoch": epoch, "model_state_dict": self.wf.state_dict(),
@@ -259,7 +289,7 @@ class Solver(SolverBase):
                     log.info("Error : Nan detected in local energy")
                     return cumulative_loss
                 self.store_observable(lpos, local_energy=eloc, ibatch=ibatch)
-            self.opt.step()
+            self.optimization_step(lpos)
             if n == 0 or cumulative_loss < min_loss:
                 min_loss = cumulative_loss
                 self.observable.models.best = dict(self.wf.state_dict())
