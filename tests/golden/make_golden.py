@@ -242,9 +242,24 @@ def make_gmetropolis(reference_root):
                                     init={"method": "uniform", "min": -1, "max": 1})
     torch.manual_seed(g["seed"])
     samples = sampler(pdf, pos=torch.as_tensor(pos0), with_tqdm=False)
+    # the same sampler on the H2 sto-3g SlaterJastrow of the "h2" case
+    from qmctorch.wavefunction import SlaterJastrow
+    from qmctorch_gb300.scf import Molecule
+    atoms, unit, basis, configs, all_mo = CASES["h2"][:5]
+    torch.manual_seed(1234)
+    mol = Molecule(atoms, unit=unit, basis=basis)
+    wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)
+    h2pos0 = seeded_positions(mol, 16, seed=21)
+    hs = GeneralizedMetropolis(nwalkers=16, nstep=20, step_size=0.2, ntherm=-10, ndecor=2,
+                               nelec=mol.nelec, ndim=3,
+                               init={"method": "uniform", "min": -1, "max": 1})
+    torch.manual_seed(g["seed"] + 1)
+    h2samples = hs(wf.pdf, pos=torch.as_tensor(h2pos0), with_tqdm=False)
     out_file = os.path.join(HERE, "gmetropolis.npz")
     np.savez_compressed(out_file, a=a, c=c, pos0=pos0, samples=samples.detach().numpy(),
                         final=sampler.walkers.pos.detach().numpy(),
+                        h2_pos0=h2pos0, h2_samples=h2samples.detach().numpy(),
+                        h2_final=hs.walkers.pos.detach().numpy(),
                         **{"cfg_" + k: np.asarray(v) for k, v in GMET.items()})
     print("wrote", out_file, os.path.getsize(out_file), "bytes")
 
