@@ -124,6 +124,11 @@ class SamplerBase:
 
 
 class Metropolis(SamplerBase):
+    """metropolis.py:10-298. ``logspace=True`` selects the reference's test
+    ``min(0, log rho' - log rho) - log u >= 0`` (288-292), the same acceptance
+    rule as ``min(1, rho' / rho) - u >= 0`` up to rounding at the boundary; the
+    kernel evaluates the ratio form for both settings."""
+
     def __init__(self, nwalkers=100, nstep=1000, step_size=0.2, ntherm=-1, ndecor=1, nelec=1,
                  ndim=3, init={"min": -5, "max": 5}, move={"type": "all-elec", "proba": "normal"},
                  logspace=False, symmetry=None, cuda=False, seed=None):
