@@ -32,7 +32,8 @@ enum qmc_status {
   QMC_ERR_SCRATCH = 3,     /* scratch buffer too small */
   QMC_ERR_LAUNCH = 4,      /* CUDA launch / runtime error */
   QMC_ERR_UNSUPPORTED = 5, /* option not implemented */
-  QMC_ERR_STATIC_LIMIT = 6 /* batch needs more than QMC_STATIC_SCRATCH_BYTES (qmc_wf_psi_static) */
+  QMC_ERR_STATIC_LIMIT = 6, /* batch needs more than QMC_STATIC_SCRATCH_BYTES (qmc_wf_psi_static) */
+  QMC_ERR_TIMEOUT = 7       /* a bounded wait of a pipelined kernel ran out (qmc_mo_eval_tc_status) */
 };
 
 /* Compile-time limits of the kernels. */
@@ -190,11 +191,30 @@ int qmc_mo_eval(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* m
  * precision. Limits: nmo <= 256 and shared memory (227 KB) for two
  * 128 x 2 nao' tiles of ao and one nmo' x 2 nao' tile of W in BF16 (nao', nmo'
  * rounded up to 16; nao <= 128 at nmo <= 128 fits), else QMC_ERR_SHAPE. If a
- * pipeline wait of the kernel runs out (1 s), the rows of the CTA concerned
- * are written as NaN.
+ * pipeline wait of the kernel runs out (1 s by default), the rows of the CTA
+ * concerned are written as NaN and a device status word is set, which
+ * qmc_mo_eval_tc_status reports.
  */
 int qmc_mo_eval_tc(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* mo,
                    void* stream);
+
+/*
+ * Status of the qmc_mo_eval_tc launches issued so far on the current device:
+ * synchronizes `stream`, then returns QMC_ERR_TIMEOUT (and clears the status
+ * word) if a pipeline wait of any of them ran out, else QMC_OK. No reference
+ * counterpart (the reference has no asynchronous kernels).
+ */
+int qmc_mo_eval_tc_status(void* stream);
+
+/*
+ * Limit of each pipeline wait of qmc_mo_eval_tc, in nanoseconds, for launches
+ * issued after the call (process-wide); returns the previous limit. Default
+ * 1e9 (1 s). 0 makes every wait give up at once (the launch aborts: all rows
+ * NaN, QMC_ERR_TIMEOUT), a test of the abort path that faults nothing. The
+ * wait for the tensor core before tensor memory is released keeps 1 s. No
+ * reference counterpart.
+ */
+uint64_t qmc_set_wait_limit_ns(uint64_t ns);
 
 /*
  * Pade e-e Jastrow. jast[nw] (J), djast[nw][3][ne] (gradient, sum_grad = 0) or

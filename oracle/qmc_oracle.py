@@ -565,13 +565,14 @@ def metropolis_sigma(step_size):
 
 
 def metropolis_replay(pdf, pos0, proposals, uniforms, ntherm=-1, ndecor=1,
-                      nelec=None, move_type="all-elec", electron_index=None):
+                      nelec=None, move_type="all-elec", electron_index=None, trace=None):
     """``Metropolis.__call__`` (metropolis.py:85-177) with the random numbers
     supplied by the caller: ``proposals[istep, (iel), w, :]`` are the
     displacements (all-elec: (nstep, nw, 3*ne); single-electron moves:
     (nstep, nmove, nw, 3)) and ``uniforms[istep, (imove), w]`` the accept
     draws. Returns (snapshots (nsnap*nw, 3ne), accepted count, accept mask
-    history)."""
+    history). With a list ``trace``, each move appends (positions before the
+    move, min(1, ratio) of the move) for decision-level comparisons."""
     eps = 1e-16
     pos = np.array(pos0, dtype=np.float64, copy=True)
     nw = pos.shape[0]
@@ -604,6 +605,8 @@ def metropolis_replay(pdf, pos0, proposals, uniforms, ntherm=-1, ndecor=1,
             fxn[fxn == 0.0] = eps
             df = fxn / fx
             df[df > 1] = 1.0
+            if trace is not None:
+                trace.append((pos.copy(), df.copy()))
             idx = (df - u) >= 0
             pos[idx] = xn[idx]
             fx[idx] = fxn[idx]

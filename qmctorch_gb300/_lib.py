@@ -124,6 +124,8 @@ SIGNATURES = {
                                    c_void_p, c_void_p]),
     "qmc_mo_eval": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_mo_eval_tc": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
+    "qmc_mo_eval_tc_status": (ctypes.c_int, [c_void_p]),
+    "qmc_set_wait_limit_ns": (ctypes.c_uint64, [ctypes.c_uint64]),
     "qmc_jastrow_ee": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                       c_void_p, c_int32, c_void_p]),
     "qmc_slater": (ctypes.c_int, [_P(WfDesc), c_void_p, c_void_p, c_int32, c_int64, c_void_p,

@@ -20,6 +20,7 @@ const char* qmc_status_string(int s) {
     case QMC_ERR_UNSUPPORTED: return "unsupported option";
     case QMC_ERR_STATIC_LIMIT:
       return "batch needs more scratch than the static array of qmc_wf_psi_static holds";
+    case QMC_ERR_TIMEOUT: return "a bounded pipeline wait of a kernel ran out (results are NaN)";
     default: return "unknown status";
   }
 }

@@ -27,13 +27,17 @@
 //               lanes 32 (w % 4) .. + 31; the two groups of four alternate
 //               16-column chunks) and FP64 stores of the MO rows.
 // So the loads of tile i + 1, the MMAs of tile i and the stores of tile i - 1
-// overlap. Every mbarrier wait is bounded (1 s); on a timeout the CTA raises
-// a shared abort flag, all roles leave their loops, the CTA's tiles are
-// written as NaN, and TMEM is released after a bounded wait for the tensor
-// core.
+// overlap. Every pipeline wait is bounded (1 s by default, host-settable
+// with qmc_set_wait_limit_ns); on a timeout the CTA raises a shared abort
+// flag, all roles leave their loops, the CTA's tiles are written as NaN, the
+// device status word g_tc_timeout is set (read and cleared by
+// qmc_mo_eval_tc_status), and TMEM is released after a wait of the default
+// limit for the last committed MMA chain.
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
+
+#include <atomic>
 
 #include "qmc_host.cuh"
 
@@ -49,7 +53,10 @@ constexpr int kThreads = kWarps * 32;   // 544
 constexpr int kProducerThreads = kProducerWarps * 32;
 constexpr int kEpilogueThreads = kEpilogueWarps * 32;
 constexpr int kMaxN = 256;              // MMA N limit for M = 128
-constexpr uint64_t kWaitNs = 1000000000ull;  // mbarrier wait limit: 1 s
+constexpr uint64_t kWaitNs = 1000000000ull;  // default pipeline wait limit: 1 s
+
+// Set by a CTA whose pipeline wait ran out (one word per device).
+__device__ int g_tc_timeout = 0;
 
 struct Shape {
   int kp;        // K of one piece (nao rounded up to 16)
@@ -107,9 +114,15 @@ __device__ inline uint64_t global_ns() {
 }
 
 // Bounded wait for the completion of phase `parity` of the mbarrier at
-// shared address `bar`. Returns false after kWaitNs or when another thread
-// raised the abort flag (and then raises it itself).
-__device__ inline bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag) {
+// shared address `bar`. Returns false after limit_ns or when another thread
+// raised the abort flag (and then raises it itself). A limit of 0 gives up at
+// once, without polling (the pipeline aborts deterministically).
+__device__ inline bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* abort_flag,
+                                 uint64_t limit_ns) {
+  if (limit_ns == 0) {
+    *abort_flag = 1;
+    return false;
+  }
   const uint64_t t0 = global_ns();
   while (true) {
     uint32_t done;
@@ -121,7 +134,7 @@ __device__ inline bool mbar_wait(uint32_t bar, uint32_t parity, volatile int* ab
         : "memory");
     if (done) return true;
     if (*abort_flag) return false;
-    if (global_ns() - t0 > kWaitNs) {
+    if (global_ns() - t0 > limit_ns) {
       *abort_flag = 1;
       return false;
     }
@@ -212,14 +225,15 @@ __device__ inline void load8(const double* __restrict__ ao, int64_t row, int64_t
 // finish the last committed MMA chain before TMEM is released.
 __device__ inline void mbar_wait_final(uint32_t bar, uint32_t parity) {
   volatile int never = 0;
-  mbar_wait(bar, parity, &never);
+  mbar_wait(bar, parity, &never, kWaitNs);
 }
 
 __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __restrict__ ao,
                                                             int64_t nrows, int nao, int nmo,
                                                             const double* __restrict__ mo_scf,
                                                             const double* __restrict__ mo_mod,
-                                                            double* __restrict__ mo, int vec) {
+                                                            double* __restrict__ mo, int vec,
+                                                            uint64_t wait_ns) {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   const Shape S = shape(nao, nmo);
   // 1 KB-aligned base (the dynamic shared-memory window is only 16-byte aligned)
@@ -284,7 +298,8 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
     int i = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = i & 1, use = i >> 1;
-      if (use > 0 && !mbar_wait(bars + 8 * (kBarEmpty + b), (uint32_t)((use - 1) & 1), abort_flag))
+      if (use > 0 &&
+          !mbar_wait(bars + 8 * (kBarEmpty + b), (uint32_t)((use - 1) & 1), abort_flag, wait_ns))
         break;
       const int64_t row0 = tile * kM;
       unsigned char* A = smem + S.a_off[b];
@@ -318,9 +333,9 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
       int i = 0;
       for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
         const int b = i & 1, use = i >> 1;
-        if (!mbar_wait(bars + 8 * (kBarFull + b), (uint32_t)(use & 1), abort_flag)) break;
-        if (use > 0 &&
-            !mbar_wait(bars + 8 * (kBarDEmpty + b), (uint32_t)((use - 1) & 1), abort_flag))
+        if (!mbar_wait(bars + 8 * (kBarFull + b), (uint32_t)(use & 1), abort_flag, wait_ns)) break;
+        if (use > 0 && !mbar_wait(bars + 8 * (kBarDEmpty + b), (uint32_t)((use - 1) & 1),
+                                  abort_flag, wait_ns))
           break;
         fence_after_sync();
         const uint32_t dt = tmem + (uint32_t)(b * S.acc_cols);
@@ -351,7 +366,7 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
     int i = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int d = i & 1, use = i >> 1;
-      bool ok = mbar_wait(bars + 8 * (kBarDFull + d), (uint32_t)(use & 1), abort_flag);
+      bool ok = mbar_wait(bars + 8 * (kBarDFull + d), (uint32_t)(use & 1), abort_flag, wait_ns);
       ok = __all_sync(0xffffffffu, ok);  // tcgen05.ld below needs the whole warp
       if (!ok) break;
       fence_after_sync();
@@ -384,8 +399,10 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
   __syncthreads();
   fence_after_sync();
   if (*abort_flag) {
-    // a wait ran out: this CTA's rows are written as NaN, and the tensor core
-    // gets a bounded wait for its last committed chain before TMEM is freed
+    // a wait ran out: this CTA's rows are written as NaN, the status word is
+    // set, and the tensor core gets a bounded wait for its last committed
+    // chain before TMEM is freed
+    if (tid == 0) atomicExch(&g_tc_timeout, 1);
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x)
       for (int idx = tid; idx < kM * nmo; idx += kThreads) {
         const int64_t row = tile * kM + idx / nmo;
@@ -407,7 +424,32 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
 
 using namespace qmc;
 
+namespace {
+std::atomic<uint64_t> g_wait_limit_ns{qmc::tc::kWaitNs};
+}
+
 extern "C" {
+
+uint64_t qmc_set_wait_limit_ns(uint64_t ns) { return g_wait_limit_ns.exchange(ns); }
+
+int qmc_mo_eval_tc_status(void* stream) {
+  if (cudaStreamSynchronize((cudaStream_t)stream) != cudaSuccess) {
+    cudaGetLastError();
+    return QMC_ERR_LAUNCH;
+  }
+  int flag = 0;
+  if (cudaMemcpyFromSymbol(&flag, tc::g_tc_timeout, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return QMC_ERR_LAUNCH;
+  }
+  if (!flag) return QMC_OK;
+  const int zero = 0;
+  if (cudaMemcpyToSymbol(tc::g_tc_timeout, &zero, sizeof(int)) != cudaSuccess) {
+    cudaGetLastError();
+    return QMC_ERR_LAUNCH;
+  }
+  return QMC_ERR_TIMEOUT;
+}
 
 int qmc_mo_eval_tc(const qmc_wf_desc* d, const double* ao, int64_t nrows, double* mo,
                    void* stream) {
@@ -436,7 +478,7 @@ int qmc_mo_eval_tc(const qmc_wf_desc* d, const double* ao, int64_t nrows, double
   if (grid > ntiles) grid = ntiles;
   const int vec = (d->nmo % 2 == 0) && ((reinterpret_cast<uintptr_t>(mo) & 15) == 0);
   tc::mo_tc_kernel<<<(unsigned)grid, tc::kThreads, S.smem, (cudaStream_t)stream>>>(
-      ao, nrows, d->nao, d->nmo, d->mo_scf, d->mo_modifier, mo, vec);
+      ao, nrows, d->nao, d->nmo, d->mo_scf, d->mo_modifier, mo, vec, g_wait_limit_ns.load());
   return launch_status();
 }
 

@@ -56,13 +56,13 @@ class GeneralizedMetropolis(SamplerBase):
             self.walkers.initialize(pos=pos)
             xi = self.walkers.pos.clone()
             rhoi = pdf(xi)
-            drifti = self.get_drift(pdf, xi)
+            drifti = self.get_drift(pdf, xi, rho=rhoi)
             rhoi[rhoi == 0] = 1e-16
             out, rate, idecor = [], 0.0, 0
             for istep in range(self.nstep):
                 xf = self.move(drifti)
                 rhof = pdf(xf)
-                driftf = self.get_drift(pdf, xf)
+                driftf = self.get_drift(pdf, xf, rho=rhof)
                 rhof[rhof == 0.0] = 1e-16
                 tif = self.trans(xi, xf, driftf)
                 tfi = self.trans(xf, xi, drifti)
@@ -109,15 +109,18 @@ class GeneralizedMetropolis(SamplerBase):
         a = (xf - xi - drifti * self.step_size).norm(dim=1)
         return torch.exp(-0.5 * a / self.step_size)
 
-    def get_drift(self, pdf, x):
+    def get_drift(self, pdf, x, rho=None):
         """grad(rho) / (2 rho) (generalized_metropolis.py:180-197): by the
         wave function's Jacobi gradient kernel when ``pdf`` is the bound pdf
-        of a wave function of this package, else by autograd."""
+        of a wave function of this package, else by autograd. ``rho`` = pdf(x)
+        when the caller has it already (the Jacobi path then makes one kernel
+        call, the gradient)."""
         owner = getattr(pdf, "__self__", None)
         if owner is not None and hasattr(owner, "gradients_jacobi"):
-            rho = pdf(x).view(-1, 1)
+            if rho is None:
+                rho = pdf(x)
             grad_rho = pdf(x, return_grad=True)
-            return 0.5 * grad_rho / rho
+            return 0.5 * grad_rho / rho.view(-1, 1)
         with torch.enable_grad():
             xg = x.detach().requires_grad_(True)
             rho = pdf(xg).view(-1, 1)

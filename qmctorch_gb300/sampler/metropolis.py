@@ -8,6 +8,11 @@ steps (proposal, psi re-evaluation, accept/reject, snapshot), with a Philox
 counter-based generator seeded per sampler. Walker initialisation mirrors the
 reference's host-side RNG calls, so a seeded initial configuration is the
 reference's.
+
+Any other density callable (an analytic pdf, a user model) is sampled by the
+reference's own algorithm as a host loop of torch operations on the walkers'
+device, with the reference's random draws (torch's generators, in its order),
+so that a seeded chain is the reference's chain.
 """
 from __future__ import annotations
 
@@ -137,11 +142,24 @@ class Metropolis(SamplerBase):
         self.logspace = logspace
         self.configure_move(move)
         self.symmetry = (lambda x: x) if symmetry is None else symmetry
-        if seed is None:
-            seed = int(torch.randint(0, 2 ** 62, (1,)).item())
-        self.seed = int(seed)
+        self._seed = None if seed is None else int(seed)
         self._step_counter = 0
         self.last_acceptance = None
+
+    @property
+    def seed(self):
+        """Key of the kernel's Philox generator. Without a ``seed`` argument it
+        is drawn from torch's generator at the first kernel launch, not at
+        construction, so that building a sampler draws nothing (the host loop
+        of an arbitrary density then sees torch's generator as the reference
+        does)."""
+        if self._seed is None:
+            self._seed = int(torch.randint(0, 2 ** 62, (1,)).item())
+        return self._seed
+
+    @seed.setter
+    def seed(self, value):
+        self._seed = int(value)
 
     def configure_move(self, move):
         """metropolis.py:179-225."""
@@ -157,13 +175,22 @@ class Metropolis(SamplerBase):
         self._move_per_iter = self.nelec if self.movedict["type"] == "all-elec-iter" else 1
         self.fixed_id_elec_list = (range(self.nelec) if self.movedict["type"] == "all-elec-iter"
                                    else [None])
+        # proposal law of the host loop (a construction draws nothing)
+        self._normal = None
+        if self.movedict["proba"] == "normal":
+            var = self.step_size / (2 * torch.sqrt(2 * torch.log(torch.as_tensor(2.0))))
+            self._normal = MultivariateNormal(torch.zeros(self.ndim), var * torch.eye(self.ndim))
 
-    def _wavefunction(self, pdf):
+    def _wavefunction(self, pdf, required=True):
+        """The wave function whose bound ``pdf`` this is, or None (or
+        TypeError when ``required``) for any other callable."""
         wf = getattr(pdf, "__self__", None)
         from ..wavefunction.slater_jastrow import SlaterJastrow
         if not isinstance(wf, SlaterJastrow) or getattr(pdf, "__name__", "") != "pdf":
-            raise TypeError("Metropolis samples the pdf of a qmctorch_gb300 wave function: "
-                            "pass wf.pdf")
+            if required:
+                raise TypeError("device-resident sampling needs the pdf of a qmctorch_gb300 "
+                                "wave function: pass wf.pdf")
+            return None
         return wf
 
     def nsnap(self):
@@ -227,8 +254,14 @@ class Metropolis(SamplerBase):
 
         ``replay`` (tests) = dict(proposals=..., uniforms=..., electron_index=...)
         replaces the generator with the caller's random numbers, in the
-        layouts of ``qmc_metropolis_args``."""
-        wf = self._wavefunction(pdf)
+        layouts of ``qmc_metropolis_args``. A ``pdf`` that is not a wave
+        function of this package is sampled by the host loop
+        (:meth:`_sample_density`)."""
+        wf = self._wavefunction(pdf, required=False)
+        if wf is None:
+            if replay is not None:
+                raise ValueError("replay inputs apply to the wave-function kernel only")
+            return self._sample_density(pdf, pos, with_tqdm)
         if self.ntherm >= self.nstep:
             raise ValueError("Thermalisation longer than trajectory")
         if self.ntherm < 0:
@@ -266,3 +299,87 @@ class Metropolis(SamplerBase):
             out = samples[:nsnap].reshape(nsnap * nw, -1)
         out = out.to(device=out_device, dtype=out_dtype)
         return self.symmetry(out).requires_grad_()
+
+    # ------------------------------------------------------------------
+    # host loop for an arbitrary density (metropolis.py:85-298)
+    # ------------------------------------------------------------------
+    def _sample_density(self, pdf, pos, with_tqdm):
+        """Metropolis chain of any callable ``pdf`` (positions -> density) on
+        the walkers' device: proposals, density calls and acceptance as the
+        reference takes them, including its random draws, so that with the
+        same torch seed the chain is the reference's."""
+        eps = 1e-7 if torch.get_default_dtype() == torch.float32 else 1e-16
+        if self.ntherm >= self.nstep:
+            raise ValueError("Thermalisation longer than trajectory")
+        with torch.no_grad():
+            if self.ntherm < 0:
+                self.ntherm = self.nstep + self.ntherm
+            self.walkers.initialize(pos=pos)
+            if self.logspace:
+                def density(x):
+                    return torch.log(pdf(x))
+            else:
+                density = pdf
+            fx = density(self.walkers.pos)
+            fx[fx == 0] = eps
+            kept, naccept = [], 0
+            tstart = time.time()
+            for istep in range(self.nstep):
+                for ielec in self.fixed_id_elec_list:
+                    trial = self._trial_positions(ielec)
+                    ftrial = density(trial)
+                    if self.logspace:
+                        ratio = ftrial - fx
+                    else:
+                        ftrial[ftrial == 0.0] = eps
+                        ratio = ftrial / fx
+                    take = self._accept_ratio(ratio)
+                    naccept += int(take.sum())
+                    self.walkers.pos[take, :] = trial[take, :]
+                    fx[take] = ftrial[take]
+                    fx[fx == 0] = eps
+                if istep >= self.ntherm and (istep - self.ntherm) % self.ndecor == 0:
+                    kept.append(self.walkers.pos.to("cpu").clone())
+            self.last_acceptance = naccept / max(
+                1, self.walkers.nwalkers * self._move_per_iter * self.nstep)
+            if with_tqdm:
+                dt = time.time() - tstart
+                log.info("   Acceptance rate     : %1.2f %%", self.last_acceptance * 100)
+                log.info("   Timing statistics   : %1.2f steps/sec.", self.nstep / dt)
+        return self.symmetry(torch.cat(kept)).requires_grad_()
+
+    def _trial_positions(self, ielec):
+        """Trial walkers: every electron displaced (all-elec, or one electron
+        in total), else one electron per walker, ``ielec`` or a random one
+        (metropolis.py:227-254)."""
+        nw = self.walkers.nwalkers
+        if self.nelec == 1 or self.movedict["type"] == "all-elec":
+            return self.walkers.pos + self._displacement(self.nelec)
+        trial = self.walkers.pos.clone().view(nw, self.nelec, self.ndim)
+        if ielec is None:
+            which = torch.LongTensor(nw).random_(0, self.nelec)
+        else:
+            which = torch.LongTensor(nw).fill_(ielec)
+        trial[range(nw), which, :] += self._displacement(1)
+        return trial.view(nw, self.nelec * self.ndim)
+
+    def _displacement(self, nmoved):
+        """(nwalkers, 3 nmoved) displacements: uniform in [-step, step] or the
+        normal law of ``configure_move`` (metropolis.py:256-277)."""
+        nw = self.walkers.nwalkers
+        if self._normal is None:
+            u = torch.rand((nw, nmoved, self.ndim), device=self.device)
+            return self.step_size * (2.0 * u.view(nw, nmoved * self.ndim) - 1.0)
+        d = self._normal.sample((nw, nmoved)).to(self.device)
+        return d.view(nw, nmoved * self.ndim)
+
+    def _accept_ratio(self, ratio):
+        """min(1, r) - u >= 0, or min(0, log r) - log u >= 0 with logspace
+        (metropolis.py:279-298); u drawn like the ratio."""
+        if self.logspace:
+            ratio[ratio > 0] = 0.0
+            tau = torch.log(torch.rand_like(ratio))
+        else:
+            ratio[ratio > 1] = 1.0
+            tau = torch.rand_like(ratio)
+        return (ratio - tau >= 0).reshape(-1).type(torch.bool)

@@ -178,6 +178,10 @@ class MolecularOrbitals(nn.Module):
         call = rt.build_desc(device, self._ao_module, mo=self)
         out = torch.empty((x.shape[0], self.mo_scf.shape[1]), dtype=rt.F64, device=device)
         fn = "qmc_mo_eval_tc" if self.precision == "mixed" else "qmc_mo_eval"
-        _lib.check(getattr(_lib.lib(), fn)(call.ref, rt.ptr(x), x.shape[0], rt.ptr(out),
-                                           rt.stream_handle()), fn)
+        lib = _lib.lib()
+        _lib.check(getattr(lib, fn)(call.ref, rt.ptr(x), x.shape[0], rt.ptr(out),
+                                    rt.stream_handle()), fn)
+        if fn == "qmc_mo_eval_tc":
+            # the pipelined kernel reports a wait that ran out by a status word
+            _lib.check(lib.qmc_mo_eval_tc_status(rt.stream_handle()), fn)
         return out.reshape(*ao.shape[:-1], -1).to(device=ao.device, dtype=ao.dtype)

@@ -5,6 +5,9 @@ Usage (in a container where the reference source tree is available):
 
     python tests/golden/make_golden.py /path/to/QMCTorch [case ...]
 
+The reference root may also come from the environment variable
+``QMCTORCH_REFERENCE`` (then every argument is a case name).
+
 Writes ``tests/golden/<case>.npz``. Each file holds the molecule / basis
 namespace (``mol_*`` / ``basis_*`` keys, the layout of
 ``qmctorch_gb300.scf.Molecule.save``), the seeded walker positions and the
@@ -264,11 +267,94 @@ def make_gmetropolis(reference_root):
     print("wrote", out_file, os.path.getsize(out_file), "bytes")
 
 
+# Walker initialisation of the reference (walkers.py:41-150): positions drawn
+# with torch's and numpy's global generators seeded before each call.
+WALKER_CASES = ("h2o_sd", "lih_cas")
+WALKER_METHODS = ("atomic", "center", "uniform", "normal")
+WALKER_SEEDS = (31, 32)  # torch.manual_seed, np.random.seed
+WALKER_NW = 40
+
+
+def make_walkers(reference_root):
+    ref_stubs.install(reference_root)
+    import torch
+    from qmctorch.sampler.walkers import Walkers
+    from qmctorch.utils import set_torch_double_precision
+    from qmctorch_gb300.scf import Molecule
+
+    set_torch_double_precision()
+    out = {}
+    for name in WALKER_CASES:
+        atoms, unit, basis = CASES[name][:3]
+        mol = Molecule(atoms, unit=unit, basis=basis)
+        for method in WALKER_METHODS:
+            torch.manual_seed(WALKER_SEEDS[0])
+            np.random.seed(WALKER_SEEDS[1])
+            w = Walkers(nwalkers=WALKER_NW, nelec=mol.nelec, ndim=3, init=mol.domain(method))
+            w.initialize()
+            out["%s_%s" % (name, method)] = w.pos.detach().numpy()
+    out_file = os.path.join(HERE, "walkers.npz")
+    np.savez_compressed(out_file, **out)
+    print("wrote", out_file, os.path.getsize(out_file), "bytes")
+
+
+# Chains of the reference Metropolis sampler on an arbitrary density (the
+# analytic one of the drift-diffusion fixture): every move type, both proposal
+# distributions and the logspace acceptance, random draws from torch's
+# generator seeded before each call.
+MGEN = {"nwalkers": 16, "nelec": 2, "ndim": 3, "nstep": 24, "step_size": 0.4,
+        "ntherm": -8, "ndecor": 2, "seed": 4040}
+MGEN_CASES = (("all-elec", "normal", False), ("one-elec", "uniform", False),
+              ("all-elec-iter", "normal", False), ("all-elec", "normal", True),
+              ("one-elec", "normal", False), ("all-elec-iter", "uniform", True))
+
+
+def make_metropolis_generic(reference_root):
+    ref_stubs.install(reference_root)
+    import torch
+    from qmctorch.sampler import Metropolis
+    from qmctorch.utils import set_torch_double_precision
+
+    set_torch_double_precision()
+    a, c = gmet_density_params()
+    at, ct = torch.as_tensor(a), torch.as_tensor(c)
+
+    def pdf(x):
+        return torch.exp(-(at * (x - ct) ** 2).sum(-1))
+
+    g = MGEN
+    pos0 = np.random.default_rng(8).normal(size=(g["nwalkers"], g["nelec"] * g["ndim"]))
+    out = {"pos0": pos0}
+    for i, (mtype, proba, logspace) in enumerate(MGEN_CASES):
+        sampler = Metropolis(nwalkers=g["nwalkers"], nstep=g["nstep"], step_size=g["step_size"],
+                             ntherm=g["ntherm"], ndecor=g["ndecor"], nelec=g["nelec"],
+                             ndim=g["ndim"], init={"method": "uniform", "min": -1, "max": 1},
+                             move={"type": mtype, "proba": proba}, logspace=logspace)
+        torch.manual_seed(g["seed"] + i)
+        samples = sampler(pdf, pos=torch.as_tensor(pos0).clone(), with_tqdm=False)
+        out["samples_%d" % i] = samples.detach().numpy()
+        out["final_%d" % i] = sampler.walkers.pos.detach().numpy()
+    out_file = os.path.join(HERE, "metropolis_generic.npz")
+    np.savez_compressed(out_file, **out)
+    print("wrote", out_file, os.path.getsize(out_file), "bytes")
+
+
+EXTRA = {"gmetropolis": "make_gmetropolis", "walkers": "make_walkers",
+         "metropolis_generic": "make_metropolis_generic"}
+
+
 if __name__ == "__main__":
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
-    names = tuple(sys.argv[2:])
-    if "gmetropolis" in names or not names:
-        make_gmetropolis(root)
-    names = tuple(n for n in names if n != "gmetropolis")
-    if names or len(sys.argv) <= 2:
+    args = sys.argv[1:]
+    root = os.environ.get("QMCTORCH_REFERENCE")
+    if root is None:
+        if not args:
+            sys.exit("usage: make_golden.py REFERENCE_ROOT [case ...] "
+                     "(or set QMCTORCH_REFERENCE)")
+        root, args = args[0], args[1:]
+    names = tuple(args)
+    for extra, fn in EXTRA.items():
+        if extra in names or not names:
+            globals()[fn](root)
+    names = tuple(n for n in names if n not in EXTRA)
+    if names or not args:
         main(root, names)

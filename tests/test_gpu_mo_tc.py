@@ -88,3 +88,42 @@ def test_tensor_core_mo_is_deterministic_and_follows_mo_modifier():
         wfmx.mo.mo_modifier.data.copy_(mod.to(wfmx.mo.mo_modifier.device))
         wf64.mo.mo_modifier.data.copy_(mod.to(wf64.mo.mo_modifier.device))
         check_close(wfmx.mo(ao), wf64.mo(ao), ao, wf64)
+
+
+def test_tensor_core_mo_reports_a_wait_that_ran_out():
+    """With a pipeline wait limit of 0 every wait of the kernel gives up at
+    once (nothing is waited for; no fault, no hang): the launch writes NaN
+    rows, qmc_mo_eval_tc_status returns QMC_ERR_TIMEOUT and clears the status
+    word, the module call raises, and with the default limit restored the
+    next call is exact again."""
+    from qmctorch_gb300 import _lib
+    mol, d = load("h2o_sd")
+    wfmx = make_wf(mol, d, "mixed")
+    wf64 = make_wf(mol, d, "fp64")
+    x = seeded_positions(mol, 4096, seed=11)
+    lib = _lib.lib()
+    stream = torch.cuda.current_stream().cuda_stream
+    with torch.no_grad():
+        ao = wf64.ao(x)
+        mo64 = wf64.mo(ao)
+        assert lib.qmc_mo_eval_tc_status(stream) == 0
+        old = lib.qmc_set_wait_limit_ns(0)
+        try:
+            assert old == 1000000000
+            with pytest.raises(_lib.QMCError, match="ran out"):
+                wfmx.mo(ao)
+            # the same launch through the C ABI: NaN rows and the status word
+            from qmctorch_gb300.wavefunction import runtime as rt
+            call = rt.build_desc(ao.device, wfmx.mo._ao_module, mo=wfmx.mo)
+            a2 = ao.reshape(-1, ao.shape[-1]).contiguous()
+            out = torch.zeros((a2.shape[0], mo64.shape[-1]), dtype=torch.float64,
+                              device=ao.device)
+            st = lib.qmc_mo_eval_tc(call.ref, a2.data_ptr(), a2.shape[0], out.data_ptr(), stream)
+            assert st == 0
+            assert lib.qmc_mo_eval_tc_status(stream) == 7
+            assert bool(torch.isnan(out).all())
+            assert lib.qmc_mo_eval_tc_status(stream) == 0  # cleared
+        finally:
+            lib.qmc_set_wait_limit_ns(old)
+        check_close(wfmx.mo(ao), mo64, ao, wf64)
+        assert lib.qmc_mo_eval_tc_status(stream) == 0

@@ -224,3 +224,16 @@ def test_tensor_core_mo_rejects_bad_arguments_and_shapes_without_a_gpu():
         assert SlaterJastrow(mol, precision="mixed").mo.precision == "mixed"
     finally:
         torch.set_default_dtype(old)
+
+
+def test_pipeline_wait_limit_is_host_settable_without_a_gpu():
+    """qmc_set_wait_limit_ns stores the limit of the tensor-core kernel's
+    pipeline waits for later launches and returns the previous one."""
+    lib = _lib.lib()
+    old = lib.qmc_set_wait_limit_ns(12345)
+    try:
+        assert old == 1000000000
+        assert lib.qmc_set_wait_limit_ns(0) == 12345
+    finally:
+        lib.qmc_set_wait_limit_ns(old)
+    assert lib.qmc_status_string(7).startswith(b"a bounded pipeline wait")
