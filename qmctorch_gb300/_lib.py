@@ -24,6 +24,10 @@ INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
            "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu", "qmc_reduce.cu", "qmc_mo_tc.cu"]
+# translation units compiled more than once, with defines: (source, object, flags)
+INSTANCES = [("qmc_metropolis_inst.cu", "qmc_metropolis_%s_%d" % (r, jc),
+              ["-DQMC_INST_R=%s" % r, "-DQMC_INST_JC=%d" % jc])
+             for r in ("float", "double") for jc in (8, 16, 24)]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I" + INCLUDE]
 
@@ -49,9 +53,10 @@ def build(force=False, verbose=False):
     os.makedirs(LIBDIR, exist_ok=True)
     nvcc = _nvcc()
 
-    def compile_one(src):
-        obj = os.path.join(BUILD, src.replace(".cu", ".o"))
-        cmd = [nvcc] + ARCH + NVCC_FLAGS + ["-c", os.path.join(CSRC, src), "-o", obj]
+    def compile_one(unit):
+        src, name, flags = unit
+        obj = os.path.join(BUILD, name + ".o")
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + flags + ["-c", os.path.join(CSRC, src), "-o", obj]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("nvcc failed for %s:\n%s%s" % (src, r.stdout, r.stderr))
@@ -59,8 +64,11 @@ def build(force=False, verbose=False):
             print(r.stdout + r.stderr)
         return obj
 
-    with ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
-        objs = list(ex.map(compile_one, SOURCES))
+    units = [(src, src[:-3], []) for src in SOURCES] + INSTANCES
+    # longest first: the Metropolis and sweep units set the wall time
+    units.sort(key=lambda u: ("inst" not in u[0], "sweep" not in u[0]))
+    with ThreadPoolExecutor(max_workers=min(len(units), os.cpu_count() or 4)) as ex:
+        objs = list(ex.map(compile_one, units))
     tmp = LIBPATH + ".tmp"
     cmd = [nvcc] + ARCH + ["-shared", "-cudart", "shared", "-Xlinker",
                            "-rpath,/usr/local/cuda/lib64", "-o", tmp] + objs

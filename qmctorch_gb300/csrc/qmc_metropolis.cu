@@ -1,227 +1,26 @@
-// Persistent Metropolis sampler (one thread per walker chain).
+// Persistent Metropolis sampler: C entry points (kernels in qmc_metropolis.cuh).
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include "qmc_ep.cuh"
-#include "qmc_host.cuh"
-#include "qmc_rng.cuh"
+#include "qmc_metropolis.cuh"
 
-#include <mutex>
-
+// instantiated in qmc_metropolis_inst.cu (one translation unit per pair)
 namespace qmc {
-
-// One block advances `nwb` walker chains through all steps. Per move: every
-// electron thread writes its proposed coordinates (Philox normals or the
-// replay input), the block evaluates psi at the proposal (qmc_ep.cuh), the
-// walker's combine thread takes the accept decision, and the electron threads
-// copy accepted coordinates. Generator: counter (call, walker, step), key
-// (seed); call = move * (nelec + 2) + e for electron e's three normals,
-// + nelec for the accept uniform, + nelec + 1 for the one-elec electron index.
-template <typename R, int JC>
-__device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc_metropolis_args& a,
-                                                 unsigned char* __restrict__ scr, int64_t ss,
-                                                 const EPShape& S, int64_t block,
-                                                 unsigned char* smem) {
-  const Tables<R> t = load_tables<R>(d, d.nmo_used, S.ncol, smem + S.o_tab);
-  const int64_t nw = a.nwalkers;
-  const int nwb = S.nwb, ne = d.nelec, nc = 3 * ne, ps = S.pstride;
-  const int64_t w0 = block * nwb;
-  const int tid = threadIdx.x;
-  const int slot = tid / nwb, wl = tid - (tid / nwb) * nwb;
-  const int nslot = S.nslot;
-  const int64_t w = w0 + wl;
-  const bool active = slot < nslot;    // an electron slot (electrons slot, slot + nslot, ...)
-  const bool live = active && w < nw;  // ... of a real walker
-  XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);    // current positions
-  XP<R>* PN = reinterpret_cast<XP<R>*>(smem + S.o_pnew);  // proposal
-  double* PSI = reinterpret_cast<double*>(smem + S.o_psi);
-  double* F = reinterpret_cast<double*>(smem + S.o_f);
-  int* IEL = reinterpret_cast<int*>(smem + S.o_iel);
-  int* ACC = reinterpret_cast<int*>(smem + S.o_acc);
-  const EPPtrs ptrs{smem, S};
-  const double eps = 1e-16;
-  ep_stage_positions<R>(a.pos, w0, nw, nwb, nc, ps, P);
-  ep_eval<R, JC, false>(d, t, ptrs, P, scr, ss, w0, nw);
-  int nacc = 0;
-  double psi_cur = 0.0;  // combine threads: psi at the current positions
-  if (tid < nwb) {
-    psi_cur = PSI[tid];
-    const double f = psi_cur * psi_cur;
-    F[tid] = f == 0.0 ? eps : f;
-  }
-  const double sigma = a.step_size / (2.0 * sqrt(2.0 * log(2.0)));
-  const double sd = sqrt(sigma);  // MultivariateNormal(0, sigma I): std = sqrt(sigma)
-  Rng rng{(uint32_t)a.seed, (uint32_t)(a.seed >> 32), (uint32_t)w, 0, 0};
-  const int nmove = a.move_type == QMC_MOVE_ALL_ELEC_ITER ? ne : 1;
-  int64_t isnap = 0, idecor = 0;
-  for (int istep = 0; istep < a.nstep; ++istep) {
-    rng.step = a.step_offset + istep;
-    for (int im = 0; im < nmove; ++im) {
-      const uint32_t call0 = (uint32_t)im * (uint32_t)(ne + 2);
-      // which electron moves
-      if (a.move_type == QMC_MOVE_ONE_ELEC) {
-        if (tid < nwb) {
-          int iel = 0;
-          if (w0 + tid < nw) {
-            if (a.proposals) {
-              iel = a.electron_index[(int64_t)istep * nw + w0 + tid];
-            } else {
-              iel = electron_draw(rng, call0 + ne + 1, ne);
-            }
-          }
-          IEL[tid] = iel;
-        }
-        __syncthreads();
-      }
-      // proposal
-      for (int e = slot; e < ne && active; e += nslot) {
-        const bool moves = live && (a.move_type == QMC_MOVE_ALL_ELEC ||
-                                    (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]));
-        XP<R>* pn = PN + wl * ps + 3 * e;
-        const XP<R>* pc = P + wl * ps + 3 * e;
-        if (moves) {
-          const double* rp =
-              !a.proposals ? nullptr
-              : a.move_type == QMC_MOVE_ALL_ELEC
-                  ? a.proposals + ((int64_t)istep * nw + w) * nc + 3 * e
-                  : a.proposals + (((int64_t)istep * nmove + im) * nw + w) * 3;
-          propose_electron<R>(rng, call0 + e, a.proba, a.step_size, sd, rp, pc, pn);
-        } else {
-          for (int q = 0; q < 3; ++q) pn[q] = pc[q];
-        }
-      }
-      __syncthreads();
-      ep_eval<R, JC, false>(d, t, ptrs, PN, scr, ss, w0, nw);
-      // accept / reject (metropolis.py:141-160, 279-298)
-      if (tid < nwb && w0 + tid < nw) {
-        double u;
-        if (a.proposals) {
-          u = a.move_type == QMC_MOVE_ALL_ELEC
-                  ? a.uniforms[(int64_t)istep * nw + w0 + tid]
-                  : a.uniforms[((int64_t)istep * nmove + im) * nw + w0 + tid];
-        } else {
-          u = accept_uniform(rng, call0 + ne);
-        }
-        double fxn = PSI[tid] * PSI[tid];
-        if (fxn == 0.0) fxn = eps;
-        double df = fxn / F[tid];
-        if (df > 1.0) df = 1.0;
-        const int acc = (df - u >= 0.0) ? 1 : 0;
-        ACC[tid] = acc;
-        if (acc) {
-          F[tid] = fxn;
-          psi_cur = PSI[tid];
-          ++nacc;
-        }
-      }
-      __syncthreads();
-      if (live && ACC[wl])
-        for (int e = slot; e < ne; e += nslot)
-          for (int q = 0; q < 3; ++q) P[wl * ps + 3 * e + q] = PN[wl * ps + 3 * e + q];
-      __syncthreads();
-    }
-    if (istep >= a.ntherm) {
-      if (idecor % a.ndecor == 0) {
-        if (a.samples && isnap < a.nsnap && live)
-          for (int e = slot; e < ne; e += nslot) {
-            double* out = a.samples + (isnap * nw + w) * nc + 3 * e;
-            for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * ps + 3 * e + q]);
-          }
-        ++isnap;
-      }
-      ++idecor;
-    }
-  }
-  if (live)
-    for (int e = slot; e < ne; e += nslot)
-      for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * ps + 3 * e + q]);
-  if (tid < nwb && w0 + tid < nw) {
-    if (a.accepted) a.accepted[w0 + tid] += nacc;
-    if (a.psi_out) a.psi_out[w0 + tid] = psi_cur;
-  }
-}
-
-template <typename R, int JC>
-__global__ void __launch_bounds__(EPBound<R>::kThreads)
-    metropolis_kernel(const __grid_constant__ qmc_wf_desc d,
-                      const __grid_constant__ qmc_metropolis_args a, unsigned char* __restrict__ scr,
-                      int64_t ss, const __grid_constant__ EPShape S) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  metropolis_block<R, JC>(d, a, scr, ss, S, blockIdx.x, smem);
-}
-
-// Several independent jobs (molecules of one launch shape: same electron
-// count and table sizes) in one launch. The job table travels in the kernel
-// parameters; block b serves job j with block0[j] <= b < block0[j + 1].
-struct MetBatchJob {
-  qmc_wf_desc d;
-  qmc_metropolis_args a;
-  unsigned char* scr;
-  int64_t ss;
-};
-struct MetBatch {
-  int32_t njobs;
-  int64_t block0[QMC_MAX_BATCH + 1];
-  MetBatchJob job[QMC_MAX_BATCH];
-};
-
-template <typename R, int JC>
-__global__ void __launch_bounds__(EPBound<R>::kThreads)
-    metropolis_batch_kernel(const __grid_constant__ MetBatch b, const __grid_constant__ EPShape S) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int64_t bid = blockIdx.x;
-  int j = 0;
-  while (j + 1 < b.njobs && b.block0[j + 1] <= bid) ++j;
-  const MetBatchJob& J = b.job[j];
-  metropolis_block<R, JC>(J.d, J.a, J.scr, J.ss, S, bid - b.block0[j], smem);
-}
-
-template <typename R, int JC>
-static int launch_metropolis_batch(const qmc_wf_desc* descs, const qmc_metropolis_args* args,
-                                   void* const* scratch, int njobs, cudaStream_t s) {
-  int64_t nwt = 0;
-  for (int j = 0; j < njobs; ++j) nwt += args[j].nwalkers;
-  const EPShape S = ep_plan<R>(descs[0], 2, JC, metropolis_batch_kernel<R, JC>, nwt);
-  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
-  for (int j = 1; j < njobs; ++j) {
-    const EPShape Sj = ep_shape<R>(descs[j], 2, S.nwb, JC, S.nslot);
-    if (Sj.smem != S.smem || Sj.o_pos != S.o_pos || Sj.o_mo != S.o_mo || Sj.o_acc != S.o_acc ||
-        Sj.pstride != S.pstride ||
-        Sj.ncol != S.ncol || Sj.nthreads != S.nthreads)
-      return QMC_ERR_SHAPE;
-  }
-  int st = prepare_smem(metropolis_batch_kernel<R, JC>, S.smem);
-  if (st) return st;
-  static MetBatch b;  // host staging of the parameter block (copied at launch)
-  static std::mutex mu;
-  std::lock_guard<std::mutex> g(mu);
-  b.njobs = njobs;
-  b.block0[0] = 0;
-  for (int j = 0; j < njobs; ++j) {
-    b.job[j].d = descs[j];
-    b.job[j].a = args[j];
-    b.job[j].scr = (unsigned char*)scratch[j];
-    b.job[j].ss = pad_walkers(args[j].nwalkers);
-    b.block0[j + 1] = b.block0[j] + (args[j].nwalkers + S.nwb - 1) / S.nwb;
-  }
-  if (b.block0[njobs] == 0) return QMC_OK;
-  metropolis_batch_kernel<R, JC><<<(unsigned)b.block0[njobs], S.nthreads, S.smem, s>>>(b, S);
-  return launch_status();
-}
-
-template <typename R, int JC>
-static int launch_metropolis(const qmc_wf_desc* d, const qmc_metropolis_args* a, unsigned char* scr,
-                             cudaStream_t s) {
-  const EPShape S = ep_plan<R>(*d, 2, JC, metropolis_kernel<R, JC>, a->nwalkers);
-  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
-  int st = prepare_smem(metropolis_kernel<R, JC>, S.smem);
-  if (st) return st;
-  const dim3 grid((unsigned)((a->nwalkers + S.nwb - 1) / S.nwb));
-  metropolis_kernel<R, JC><<<grid, S.nthreads, S.smem, s>>>(*d, *a, scr, pad_walkers(a->nwalkers), S);
-  return launch_status();
-}
-
+#define QMC_MET_EXTERN(R, JC)                                                                  \
+  extern template int launch_metropolis<R, JC>(const qmc_wf_desc*, const qmc_metropolis_args*, \
+                                               unsigned char*, cudaStream_t);                  \
+  extern template int launch_metropolis_batch<R, JC>(const qmc_wf_desc*,                       \
+                                                     const qmc_metropolis_args*, void* const*, \
+                                                     int, cudaStream_t);
+QMC_MET_EXTERN(float, 8)
+QMC_MET_EXTERN(float, 16)
+QMC_MET_EXTERN(float, 24)
+QMC_MET_EXTERN(double, 8)
+QMC_MET_EXTERN(double, 16)
+QMC_MET_EXTERN(double, 24)
+#undef QMC_MET_EXTERN
 }  // namespace qmc
+
 
 using namespace qmc;
 

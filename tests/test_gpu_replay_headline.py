@@ -72,7 +72,7 @@ def test_fp64_chain_takes_every_decision_of_the_oracle(chain):
     gpu_acc = np.any(snaps != prev, axis=2)
     np.testing.assert_array_equal(gpu_acc, chain["acc"])
     np.testing.assert_allclose(snaps, chain["samples"], rtol=0, atol=1e-12)
-    assert 0.2 < chain["acc"].mean() < 0.95  # a chain that moves and rejects
+    assert 0.1 < chain["acc"].mean() < 0.95  # a chain that moves and rejects
 
 
 def test_mixed_decisions_differ_only_within_tolerance(chain):
