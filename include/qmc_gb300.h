@@ -113,6 +113,15 @@ typedef struct qmc_wf_desc {
   const int32_t* cfg_det[2];  /* [ncfg] spin determinant of each configuration */
   const double* ci_weight;    /* [ncfg] (fc.weight) */
   double e_nuc;               /* nuclear repulsion (wf_base.py:97-116) */
+  /* Electron-nucleus Pade Jastrow (optional): log J gains
+     sum_{i,A} r_iA / (1 + w_en r_iA), the same static weight 1 for every pair
+     (JastrowFactorElectronNuclei, jastrow_factor_electron_nuclei.py:9-161, with
+     elec_nuclei/kernels/pade_jastrow_kernel.py:8-116). use_jastrow above selects
+     the e-e factor and use_jastrow_en this one; with both, J is their product
+     (CombineJastrow, combine_jastrow.py:7-195). */
+  int32_t use_jastrow_en;
+  const double* jastrow_en_w;     /* [1] (jastrow_kernel.weight of the e-n factor) */
+  const double* jastrow_en_atoms; /* [natom*3] nucleus positions of the e-n factor */
 } qmc_wf_desc;
 
 /* Scratch bytes for nwalkers walkers; kind 0 = psi, 1 = local energy. */
@@ -226,6 +235,15 @@ int qmc_jastrow_ee(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, do
                    double* djast, double* d2jast, int32_t sum_grad, void* stream);
 
 /*
+ * Electron-nucleus Pade Jastrow factor alone (use_jastrow_en must be set):
+ * jast[nw] (J_en), djast[nw][3][ne] (sum_grad = 0) or [nw][ne] (sum_grad = 1),
+ * d2jast[nw][ne] (laplacian); NULL outputs are skipped. Replaces
+ * JastrowFactorElectronNuclei.forward (jastrow_factor_electron_nuclei.py:66-161).
+ */
+int qmc_jastrow_en(const qmc_wf_desc* d, const double* pos, int64_t nwalkers, double* jast,
+                   double* djast, double* d2jast, int32_t sum_grad, void* stream);
+
+/*
  * Slater determinants dets[nw][ncfg] from MO values mo[nw][ne][nmo_ld]
  * (SlaterPooling.forward, slater_pooling.py:64-80). If bop is not NULL, also
  * op[nw][ncfg] = Tr(A^-1 B) summed over spins for the operator matrix
@@ -252,6 +270,8 @@ int64_t qmc_adjoint_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
  *   grad_W[a*ldw+j]  += sum_w gout[w] d psi_w / d W[a][j]      (j < nmo_used,
  *                       W = mo_scf * mo_modifier; d/d mo_modifier = this * mo_scf)
  *   grad_jastrow_w[0]+= sum_w gout[w] d psi_w / d w            (if use_jastrow)
+ *   grad_jastrow_w[1]+= sum_w gout[w] d psi_w / d w_en         (if use_jastrow_en; the
+ *                       array then holds two values)
  *   grad_ci[k]       += sum_w gout[w] d psi_w / d c_k
  * weight_entry[i] maps AO weight i (ao_wd index) to its basis entry. The outputs
  * are accumulated (zero them first); the summation order over walkers is not

@@ -235,6 +235,94 @@ def jastrow_ee(pos, nup, ndown, w, derivative=0, sum_grad=True):
     raise ValueError("bad derivative")
 
 
+def jastrow_en(pos, atoms, w, derivative=0, sum_grad=True):
+    """``JastrowFactorElectronNuclei.forward`` and derivatives
+    (jastrow_factor_electron_nuclei.py:66-161) with the e-n Pade kernel
+    (elec_nuclei/kernels/pade_jastrow_kernel.py:8-116, static weight 1) and the
+    quadratic-form electron-nucleus distance (electron_nuclei_distance.py:60-190,
+    eps 1e-16 in the derivative denominators)."""
+    pos = np.asarray(pos, dtype=np.float64)
+    atoms = np.asarray(atoms, dtype=np.float64).reshape(-1, 3)
+    nb = pos.shape[0]
+    p = pos.reshape(nb, -1, 3)
+    eps = 1e-16
+    norm = (p ** 2).sum(-1)[..., None]                     # (nb, ne, 1)
+    norm_at = (atoms ** 2).sum(-1)[None, None, :]          # (1, 1, na)
+    r = np.sqrt(norm + norm_at - 2.0 * p @ atoms.T)        # (nb, ne, na)
+    kern = r / (1.0 + w * r)
+    jast = np.exp(kern.sum((-1, -2)))[:, None]
+    if derivative == 0:
+        return jast
+    diff = p[:, :, :, None] - atoms.T[None, None]          # (nb, ne, 3, na)
+    dr = np.transpose(diff / (r[:, :, None, :] + eps), (0, 2, 1, 3))  # (nb, 3, ne, na)
+    r_ = r[:, None]
+    denom = 1.0 / (1.0 + w * r_)
+    dker = dr * denom - w * r_ * dr * denom ** 2           # compute_derivative 48-82
+
+    def first():
+        if sum_grad:
+            return dker.sum((1, 3)) * jast
+        return dker.sum(3) * jast[:, :, None]
+
+    def second():
+        d2 = np.transpose(diff ** 2, (0, 2, 1, 3))         # (nb, 3, ne, na)
+        d2 = np.stack([d2[:, 1] + d2[:, 2], d2[:, 2] + d2[:, 0], d2[:, 0] + d2[:, 1]], axis=1)
+        d2r = d2 / (r[:, None] ** 3 + eps)
+        drs = dr * dr
+        d2k = (d2r * denom - 2 * w * drs * denom ** 2 - w * r_ * d2r * denom ** 2
+               + 2 * w ** 2 * r_ * drs * denom ** 3)       # compute_second_derivative 84-116
+        return (d2k.sum((1, 3)) + (dker.sum(3) ** 2).sum(1)) * jast
+
+    if derivative == 1:
+        return first()
+    if derivative == 2:
+        return second()
+    if list(derivative) == [0, 1, 2]:
+        return jast, first(), second()
+    raise ValueError("bad derivative")
+
+
+def combine_jastrow(terms, pos, derivative=0, sum_grad=True):
+    """``CombineJastrow.forward`` (combine_jastrow.py:38-195): the product of
+    the factors ``terms`` (callables with the (pos, derivative, sum_grad)
+    signature above) with its product-rule derivatives."""
+    def prod(v):
+        out = v[0]
+        for t in v[1:]:
+            out = out * t
+        return out
+
+    def d1(vals, grads):
+        if len(grads) == 1:
+            return grads[0]
+        return sum(prod(vals[:k] + [grads[k]] + vals[k + 1:]) for k in range(len(vals)))
+
+    def d2(vals, grads, laps):
+        if len(laps) == 1:
+            return laps[0]
+        out = sum(prod(vals[:k] + [laps[k]] + vals[k + 1:]) for k in range(len(vals)))
+        wide = [v[..., None] for v in vals]
+        for k in range(len(vals) - 1):
+            for m in range(k + 1, len(vals)):
+                t = list(wide)
+                t[k], t[m] = grads[k], grads[m]
+                out = out + 2.0 * prod(t).sum(1)
+        return out
+
+    vals = [f(pos, 0) for f in terms]
+    if derivative == 0:
+        return prod(vals)
+    if derivative == 1:
+        if sum_grad:
+            return d1(vals, [f(pos, 1, True) for f in terms])
+        return d1([v[..., None] for v in vals], [f(pos, 1, False) for f in terms])
+    grads = [f(pos, 1, False) for f in terms]
+    laps = [f(pos, 2) for f in terms]
+    if derivative == 2:
+        return d2(vals, grads, laps)
+    return prod(vals), d1([v[..., None] for v in vals], grads), d2(vals, grads, laps)
+
+
 # ----------------------------------------------------------------------------
 # CI configurations and Slater pooling
 # ----------------------------------------------------------------------------
@@ -451,7 +539,9 @@ class OracleSlaterJastrow:
 
     def __init__(self, mol_like, configs="ground_state", include_all_mo=True,
                  jastrow_w=1.0, use_jastrow=True, fc_weight=None, mo_modifier=None,
-                 bas_exp=None):
+                 bas_exp=None, jastrow_terms=None):
+        """``jastrow_terms``: list of ("ee", w) / ("en", w) factors combined as
+        CombineJastrow does; default [("ee", jastrow_w)] when use_jastrow."""
         b = mol_like.basis
         self.nup, self.ndown = int(mol_like.nup), int(mol_like.ndown)
         self.nelec = self.nup + self.ndown
@@ -475,13 +565,26 @@ class OracleSlaterJastrow:
         self.fc = np.asarray(fc_weight, dtype=np.float64).reshape(-1)
         self.use_jastrow = use_jastrow
         self.jastrow_w = float(jastrow_w)
+        if jastrow_terms is None:
+            jastrow_terms = [("ee", self.jastrow_w)] if use_jastrow else []
+        self.jastrow_terms = [(k, float(w)) for k, w in jastrow_terms]
+        self.use_jastrow = len(self.jastrow_terms) > 0
+        self.en_atoms = np.asarray(mol_like.atom_coords, dtype=np.float64)
 
     @property
     def W(self):
         return self.mo_scf * self.mo_modifier
 
+    def _factor(self, kind, w):
+        if kind == "ee":
+            return lambda pos, der=0, sg=True: jastrow_ee(pos, self.nup, self.ndown, w, der, sg)
+        return lambda pos, der=0, sg=True: jastrow_en(pos, self.en_atoms, w, der, sg)
+
     def jastrow(self, pos, derivative=0, sum_grad=True):
-        return jastrow_ee(pos, self.nup, self.ndown, self.jastrow_w, derivative, sum_grad)
+        terms = [self._factor(k, w) for k, w in self.jastrow_terms]
+        if len(terms) == 1:
+            return terms[0](pos, derivative, sum_grad)
+        return combine_jastrow(terms, pos, derivative, sum_grad)
 
     def forward(self, pos):
         """slater_jastrow.py:243-286 -> (nb, 1)."""

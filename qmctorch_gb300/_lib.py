@@ -102,6 +102,7 @@ class WfDesc(ctypes.Structure):
         ("det_mode", c_int32), ("ncfg", c_int32), ("max_orb", c_int32 * 2),
         ("ndet", c_int32 * 2), ("det_table", c_void_p * 2), ("cfg_det", c_void_p * 2),
         ("ci_weight", c_void_p), ("e_nuc", ctypes.c_double),
+        ("use_jastrow_en", c_int32), ("jastrow_en_w", c_void_p), ("jastrow_en_atoms", c_void_p),
     ]
 
 
@@ -133,6 +134,8 @@ SIGNATURES = {
     "qmc_mo_eval": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_mo_eval_tc": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_mo_eval_tc_status": (ctypes.c_int, [c_void_p]),
+    "qmc_jastrow_en": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
+                                      c_void_p, c_int32, c_void_p]),
     "qmc_set_wait_limit_ns": (ctypes.c_uint64, [ctypes.c_uint64]),
     "qmc_jastrow_ee": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                       c_void_p, c_int32, c_void_p]),

@@ -47,8 +47,10 @@ struct AdjLayout {  // per-walker scratch, in doubles (item-major)
 
 // Per-walker gradient slots: W [nao][nmu], exponents [nweight] (one per basis
 // entry), CI weights [ncfg], Pade weight [1].
+// gradient slots per walker: W, exponents, CI weights, the e-e and the e-n
+// Pade weights
 __host__ __device__ inline int64_t adj_acc_doubles(const qmc_wf_desc& d) {
-  return (int64_t)d.nao * d.nmo_used + d.nweight + d.ncfg + 1;
+  return (int64_t)d.nao * d.nmo_used + d.nweight + d.ncfg + 2;
 }
 
 __host__ __device__ inline AdjLayout adj_layout(const qmc_wf_desc& d) {
@@ -110,7 +112,14 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
           dlogj -= w0 * r * r * iu * iu;
         }
     }
-    const double J = d.use_jastrow ? exp(logj) : 1.0;
+    double dlogj_en = 0.0;  // d log J / d w_en (elec_nuclei pade_jastrow_kernel.py:48-61)
+    if (d.use_jastrow_en)
+      for (int i = 0; i < ne; ++i) {
+        const EnTerms en = en_terms(d, P(3 * i), P(3 * i + 1), P(3 * i + 2));
+        logj += en.u;
+        dlogj_en += en.du;
+      }
+    const double J = (d.use_jastrow || d.use_jastrow_en) ? exp(logj) : 1.0;
     // AO and MO values
     for (int e = 0; e < ne; ++e) {
       for_each_ao<double, false>(t, P(3 * e), P(3 * e + 1), P(3 * e + 2),
@@ -149,6 +158,7 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
       accC[k * ss] += gw * J * dd;  // d psi / d c_k
     }
     if (d.use_jastrow) accJ[0] += gw * J * psid * dlogj;  // d psi / d w
+    if (d.use_jastrow_en) accJ[ss] += gw * J * psid * dlogj_en;  // d psi / d w_en
     // d psi / d MO = J sum_u coef_u det_u A_u^-T (scattered into the columns of u)
     for (int s = 0; s < 2; ++s) {
       const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0;
@@ -303,7 +313,7 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
     const PosView P{pos + w * 3 * ne, 1};
     // Jastrow: grad U, lap U + |grad U|^2 per electron and their w-derivatives
     // (K = w0 r / (1 + w r), K' = w0 / (1 + w r)^2, K'' = -2 w w0 / (1 + w r)^3)
-    const double wj = __ldg(d.jastrow_w);
+    const double wj = d.use_jastrow ? __ldg(d.jastrow_w) : 0.0;
     for (int i = 0; i < ne; ++i) {
       double g[3] = {0.0, 0.0, 0.0}, dg[3] = {0.0, 0.0, 0.0}, lap = 0.0, dlap = 0.0;
       if (d.use_jastrow)
@@ -323,6 +333,11 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
           lap += 2.0 * k1 / r + k2;
           dlap += 2.0 * dk1 / r + dk2;
         }
+      if (d.use_jastrow_en) {
+        const EnTerms en = en_terms(d, P(3 * i), P(3 * i + 1), P(3 * i + 2));
+        for (int x = 0; x < 3; ++x) g[x] += en.g[x];
+        lap += en.lap;
+      }
       for (int x = 0; x < 3; ++x) {
         GJ(i, x) = g[x];
         DGW(i, x) = dg[x];
@@ -447,7 +462,7 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
     }
     // through B: dA_total = G_A - lapJ/2 G_B, d lapMO = -G_B/2, d gradMO = -gradU G_B;
     // Jastrow weight through grad U and lap U + |grad U|^2
-    double dwj = 0.0;
+    double dwj = 0.0, dwn = 0.0;
     for (int e = 0; e < ne; ++e) {
       double dg[3] = {0.0, 0.0, 0.0}, dl = 0.0;
       for (int j = 0; j < nmu; ++j) {
@@ -466,8 +481,18 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
         }
         dwj = fma(dl, DLW(e) + 2.0 * gdg, dwj);
       }
+      if (d.use_jastrow_en) {  // through grad U_en and lap U_en + |grad U|^2
+        const EnTerms en = en_terms(d, P(3 * e), P(3 * e + 1), P(3 * e + 2));
+        double gdg = 0.0;
+        for (int x = 0; x < 3; ++x) {
+          dwn = fma(dg[x], en.dg[x], dwn);
+          gdg = fma(GJ(e, x), en.dg[x], gdg);
+        }
+        dwn = fma(dl, en.dlap + 2.0 * gdg, dwn);
+      }
     }
     if (d.use_jastrow) accJ[0] += dwj;
+    if (d.use_jastrow_en) accJ[ss] += dwn;
     // W[a][j]: sum_e AO(e,a) dA(e,j) - (lap AO(e,a) / 2 + gradU(e) . grad AO(e,a)) G_B(e,j)
     for (int a = 0; a < nao; ++a)
       for (int j = 0; j < nmu; ++j) {
@@ -584,7 +609,7 @@ __global__ void __launch_bounds__(kAdjTPB) grad_kernel(const qmc_wf_desc d,
   double logj = 0.0;
   double* o = out + w * 3 * ne;
   for (int i = 0; i < 3 * ne; ++i) o[i] = 0.0;
-  const double wj = __ldg(d.jastrow_w);
+  const double wj = d.use_jastrow ? __ldg(d.jastrow_w) : 0.0;
   // AO values and gradients, MO rows
   for (int e = 0; e < ne; ++e) {
     for_each_ao<double, true>(t, P(3 * e), P(3 * e + 1), P(3 * e + 2),
@@ -658,12 +683,18 @@ __global__ void __launch_bounds__(kAdjTPB) grad_kernel(const qmc_wf_desc d,
                                     o[3 * (r0 + i) + q]);
     }
   }
-  // Jastrow: grad_i U (Pade kernel K' = w0 / (1 + w r)^2) and psi = J Sigma
+  // Jastrow: grad_i U (Pade kernels, K' = w0 / (1 + w r)^2 for e-e pairs and
+  // 1 / (1 + w_en r)^2 for electron-nucleus pairs) and psi = J Sigma
   double J = 1.0;
-  if (d.use_jastrow) {
+  if (d.use_jastrow || d.use_jastrow_en) {
     for (int i = 0; i < ne; ++i) {
       double g[3] = {0.0, 0.0, 0.0};
-      for (int j = 0; j < ne; ++j) {
+      if (d.use_jastrow_en) {
+        const EnTerms en = en_terms(d, P(3 * i), P(3 * i + 1), P(3 * i + 2));
+        logj += en.u;
+        for (int q = 0; q < 3; ++q) g[q] += en.g[q];
+      }
+      for (int j = 0; j < ne && d.use_jastrow; ++j) {
         if (j == i) continue;
         const double dx[3] = {P(3 * i) - P(3 * j), P(3 * i + 1) - P(3 * j + 1),
                               P(3 * i + 2) - P(3 * j + 2)};
@@ -688,7 +719,7 @@ constexpr int kRedTPB = 256;
 __global__ void __launch_bounds__(kRedTPB) adj_reduce_kernel(
     const double* __restrict__ gacc, int64_t nw, int64_t ss, int nao, int nmu, int nweight,
     int nent, int ncfg, double* __restrict__ g_W, int ldw, double* __restrict__ g_exp,
-    double* __restrict__ g_ci, double* __restrict__ g_jw) {
+    double* __restrict__ g_ci, double* __restrict__ g_jw, double* __restrict__ g_jwn) {
   __shared__ double sh[kRedTPB];
   const int64_t i = blockIdx.x;
   const double* row = gacc + i * ss;
@@ -710,8 +741,10 @@ __global__ void __launch_bounds__(kRedTPB) adj_reduce_kernel(
     if (e < nent) g_exp[e] += v;
   } else if (i < nw_ + nweight + ncfg) {
     g_ci[i - nw_ - nweight] += v;
-  } else if (g_jw) {
-    g_jw[0] += v;
+  } else if (i == nw_ + nweight + ncfg) {
+    if (g_jw) g_jw[0] += v;
+  } else if (g_jwn) {
+    g_jwn[0] += v;
   }
 }
 
@@ -751,7 +784,8 @@ int qmc_wf_psi_adjoint(const qmc_wf_desc* d0, const double* pos, int64_t nw, con
   const double* gacc = (const double*)scratch + adj_layout(dd).gacc * ss;
   adj_reduce_kernel<<<(unsigned)adj_acc_doubles(dd), kRedTPB, 0, cs>>>(
       gacc, nw, ss, dd.nao, dd.nmo_used, dd.nweight, nentries, dd.ncfg, grad_W, ldw, grad_exp,
-      grad_ci, d->use_jastrow ? grad_jastrow_w : nullptr);
+      grad_ci, d->use_jastrow ? grad_jastrow_w : nullptr,
+      d->use_jastrow_en ? grad_jastrow_w + 1 : nullptr);
   return launch_status();
 }
 
@@ -786,7 +820,8 @@ int qmc_wf_local_energy_adjoint(const qmc_wf_desc* d0, const double* pos, int64_
   const double* gacc = (const double*)scratch + el_adj_layout(dd).gacc * ss;
   adj_reduce_kernel<<<(unsigned)adj_acc_doubles(dd), kRedTPB, 0, cs>>>(
       gacc, nw, ss, dd.nao, dd.nmo_used, dd.nweight, nentries, dd.ncfg, grad_W, ldw, grad_exp,
-      grad_ci, d->use_jastrow ? grad_jastrow_w : nullptr);
+      grad_ci, d->use_jastrow ? grad_jastrow_w : nullptr,
+      d->use_jastrow_en ? grad_jastrow_w + 1 : nullptr);
   return launch_status();
 }
 

@@ -388,7 +388,7 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
   const XP<R> ex = pw[3 * e], ey = pw[3 * e + 1], ez = pw[3 * e + 2];
   R gx = (R)0, gy = (R)0, gz = (R)0, jl = (R)0;
   {
-    const R w = (R)__ldg(d.jastrow_w);
+    const R w = d.use_jastrow ? (R)__ldg(d.jastrow_w) : (R)0;
     R ks = (R)0, vs = (R)0, lp = (R)0;
     if (d.use_jastrow || KIN) {
       for (int j = KIN ? 0 : e + 1; j < ne; ++j) {
@@ -411,9 +411,29 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
         }
       }
     }
+    // electron-nucleus Pade factor: K = r / (1 + w r) for every nucleus
+    R kn = (R)0;
+    if (d.use_jastrow_en) {
+      const R wn = (R)__ldg(d.jastrow_en_w);
+      for (int A = 0; A < t.natom; ++A) {
+        const R dx = dif(ex, t.en_p[3 * A]), dy = dif(ey, t.en_p[3 * A + 1]),
+                dz = dif(ez, t.en_p[3 * A + 2]);
+        const R r = rsqrt_(dx * dx + dy * dy + dz * dz);
+        const R iu = (R)1 / ((R)1 + wn * r);
+        kn += r * iu;
+        if (KIN) {
+          const R ir = (R)1 / r;
+          const R k1 = iu * iu;  // dK/dr
+          gx += k1 * dx * ir;
+          gy += k1 * dy * ir;
+          gz += k1 * dz * ir;
+          lp += (R)2 * k1 * ir - (R)2 * wn * k1 * iu;  // 2K'/r + K''
+        }
+      }
+    }
     if (KIN) {
       jl = lp + gx * gx + gy * gy + gz * gz;  // lap(J)/J of this electron
-      *jrow = 0.5 * (double)ks;               // every pair visited from both ends
+      *jrow = 0.5 * (double)ks + (double)kn;  // e-e pairs visited from both ends
       R ven = (R)0;
       for (int A = 0; A < t.natom; ++A) {
         const R dx = dif(ex, t.atom_p[3 * A]), dy = dif(ey, t.atom_p[3 * A + 1]),
@@ -422,7 +442,7 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
       }
       *vrow = 0.5 * (double)vs + (double)ven;
     } else {
-      *jrow = (double)ks;
+      *jrow = (double)ks + (double)kn;
     }
   }
   const int64_t cs = nwb;
@@ -546,7 +566,7 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
       logj += JR[e * nwb + wl];
       if (KIN) v += VR[e * nwb + wl];
     }
-    PSI[wl] = d.use_jastrow ? psid * exp(logj) : psid;
+    PSI[wl] = (d.use_jastrow || d.use_jastrow_en) ? psid * exp(logj) : psid;
     if (KIN) {
       KINV[wl] = kin;
       V[wl] = v;

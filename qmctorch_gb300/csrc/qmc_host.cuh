@@ -30,6 +30,7 @@ static inline int check_desc(const qmc_wf_desc* d) {
     return QMC_ERR_ARG;
   if (!d->contract && !d->ao_wv) return QMC_ERR_ARG;
   if (d->use_jastrow && !d->jastrow_w) return QMC_ERR_ARG;
+  if (d->use_jastrow_en && (!d->jastrow_en_w || !d->jastrow_en_atoms)) return QMC_ERR_ARG;
   if (d->nmo_used > d->nmo || d->nmo_used < 1) return QMC_ERR_ARG;
   if (d->det_mode != QMC_DET_EXCITATION && d->det_mode != QMC_DET_EXPLICIT) return QMC_ERR_ARG;
   if (d->precision != QMC_PREC_FP64 && d->precision != QMC_PREC_MIXED) return QMC_ERR_ARG;

@@ -107,6 +107,39 @@ __global__ void __launch_bounds__(128) jastrow_kernel(const qmc_wf_desc d, const
   }
 }
 
+// Electron-nucleus Pade factor alone and its derivatives per walker
+// (JastrowFactorElectronNuclei.forward, jastrow_factor_electron_nuclei.py:66-161):
+// J = exp(sum_{i,A} K(r_iA)), grad_i J = J grad_i U, lap_i J = J (lap_i U + |grad_i U|^2).
+__global__ void __launch_bounds__(128) jastrow_en_kernel(const qmc_wf_desc d,
+                                                         const double* __restrict__ pos, int64_t nw,
+                                                         double* __restrict__ jast,
+                                                         double* __restrict__ djast,
+                                                         double* __restrict__ d2jast, int sum_grad) {
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  const int ne = d.nelec;
+  PosView P{pos + w * 3 * ne, 1};
+  double u = 0.0;
+  for (int i = 0; i < ne; ++i) u += en_terms(d, P(3 * i), P(3 * i + 1), P(3 * i + 2)).u;
+  const double J = exp(u);
+  if (jast) jast[w] = J;
+  if (!djast && !d2jast) return;
+  for (int i = 0; i < ne; ++i) {
+    const EnTerms en = en_terms(d, P(3 * i), P(3 * i + 1), P(3 * i + 2));
+    const double gx = en.g[0], gy = en.g[1], gz = en.g[2];
+    if (djast) {
+      if (sum_grad) {
+        djast[w * ne + i] = J * (gx + gy + gz);
+      } else {
+        djast[(w * 3 + 0) * ne + i] = J * gx;
+        djast[(w * 3 + 1) * ne + i] = J * gy;
+        djast[(w * 3 + 2) * ne + i] = J * gz;
+      }
+    }
+    if (d2jast) d2jast[w * ne + i] = J * (en.lap + gx * gx + gy * gy + gz * gz);
+  }
+}
+
 template <bool OP>
 __global__ void __launch_bounds__(kTPB) slater_kernel(const qmc_wf_desc d, const double* __restrict__ mo,
                                                       const double* __restrict__ bop, int ld,
@@ -214,6 +247,17 @@ int qmc_jastrow_ee(const qmc_wf_desc* d, const double* pos, int64_t nw, double* 
   jastrow_kernel<<<(unsigned)((nw + 127) / 128), 128, 0, (cudaStream_t)stream>>>(*d, pos, nw, jast,
                                                                                  djast, d2jast,
                                                                                  sum_grad);
+  return launch_status();
+}
+
+int qmc_jastrow_en(const qmc_wf_desc* d, const double* pos, int64_t nw, double* jast,
+                   double* djast, double* d2jast, int32_t sum_grad, void* stream) {
+  int st = check_desc(d);
+  if (st) return st;
+  if (!d->use_jastrow_en || nw < 0 || (nw > 0 && !pos)) return QMC_ERR_ARG;
+  if (nw == 0) return QMC_OK;
+  jastrow_en_kernel<<<(unsigned)((nw + 127) / 128), 128, 0, (cudaStream_t)stream>>>(
+      *d, pos, nw, jast, djast, d2jast, sum_grad);
   return launch_status();
 }
 

@@ -355,7 +355,7 @@ __global__ void __launch_bounds__(256, kMixed<R> ? 3 : 2)
   };
   rebuild();
 
-  const R wj = (R)__ldg(d.jastrow_w);
+  const R wj = d.use_jastrow ? (R)__ldg(d.jastrow_w) : (R)0;
   const bool ci_zero = __ldg(d.ci_weight) == 0.0;  // psi = 0: the reference accepts every move
   const double sigma = a.step_size / (2.0 * sqrt(2.0 * log(2.0)));
   const double sd = sqrt(sigma);
@@ -433,6 +433,23 @@ __global__ void __launch_bounds__(256, kMixed<R> ? 3 : 2)
           du += w0 * rn / ((R)1 + wj * rn) - w0 * ro / ((R)1 + wj * ro);
         }
         du = warp_sum<R>(du);
+      }
+      // electron-nucleus Pade factor: change of electron e's row over the nuclei
+      if (d.use_jastrow_en) {
+        const XP<R> ox = P[3 * e], oy = P[3 * e + 1], oz = P[3 * e + 2];
+        const R wn = (R)__ldg(d.jastrow_en_w);
+        R dn = (R)0;
+        for (int A = lane; A < t.natom; A += 32) {
+          const XP<R> ax = t.en_p[3 * A], ay = t.en_p[3 * A + 1], az = t.en_p[3 * A + 2];
+          R dx = dif(pn[0], ax), dy = dif(pn[1], ay), dz = dif(pn[2], az);
+          const R rn = rsqrt_(dx * dx + dy * dy + dz * dz);
+          dx = dif(ox, ax);
+          dy = dif(oy, ay);
+          dz = dif(oz, az);
+          const R ro = rsqrt_(dx * dx + dy * dy + dz * dz);
+          dn += rn / ((R)1 + wn * rn) - ro / ((R)1 + wn * ro);
+        }
+        du += warp_sum<R>(dn);
       }
       __syncwarp();
       const R ratio = Y[l];

@@ -10,8 +10,8 @@ from __future__ import annotations
 import torch
 from torch import nn
 
-from .. import _lib
-from . import runtime as rt
+from ... import _lib
+from .. import runtime as rt
 
 
 class PadeJastrowKernel(nn.Module):
@@ -61,7 +61,7 @@ class JastrowFactorElectronElectron(nn.Module):
         device = rt.cuda_device()
         assert pos.shape[1] == self.nelec * self.ndim
         if self._ao_module is None:
-            from .orbitals import AtomicOrbitals
+            from ..orbitals import AtomicOrbitals
             object.__setattr__(self, "_ao_module", AtomicOrbitals(self._mol))
         x = rt.dev64(pos, device)
         nb = x.shape[0]
@@ -85,3 +85,6 @@ class JastrowFactorElectronElectron(nn.Module):
         if derivative == 2:
             return back(d2j)
         return back(jast), back(dj), back(d2j)
+
+
+JastrowFactor = JastrowFactorElectronElectron  # name exported by qmctorch.wavefunction.jastrows.elec_elec

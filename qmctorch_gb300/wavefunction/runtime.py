@@ -79,6 +79,22 @@ class Call:
         self.ref = ctypes.byref(desc)
 
 
+def jastrow_parts(jastrow):
+    """(e-e Pade factor or None, e-n Pade factor or None) of a Jastrow module:
+    one factor, or a CombineJastrow of at most one of each. Anything else
+    raises NotImplementedError (the kernels implement these two factors)."""
+    from .jastrows import CombineJastrow, JastrowFactorElectronElectron, JastrowFactorElectronNuclei
+    if jastrow is None:
+        return None, None
+    terms = list(jastrow.jastrow_terms) if isinstance(jastrow, CombineJastrow) else [jastrow]
+    ee = [t for t in terms if isinstance(t, JastrowFactorElectronElectron)]
+    en = [t for t in terms if isinstance(t, JastrowFactorElectronNuclei)]
+    if len(ee) + len(en) != len(terms) or len(ee) > 1 or len(en) > 1:
+        raise NotImplementedError("the GB300 kernels implement the Pade e-e and e-n Jastrow "
+                                  "factors, at most one of each")
+    return (ee[0] if ee else None), (en[0] if en else None)
+
+
 def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None, nup=None,
                ndown=None, nmo_used=None, e_nuc=0.0, precision=0):
     """Fill a ``qmc_wf_desc`` from the modules of a wave function. Any module
@@ -118,14 +134,24 @@ def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None
         d.nmo = 1
         d.mo_scf = d.mo_modifier = ptr(dd)
     d.nmo_used = d.nmo if nmo_used is None else nmo_used
-    if jastrow is not None:
-        wj = dev64(jastrow.jastrow_kernel.weight, device)
+    ee, en = jastrow_parts(jastrow)
+    if ee is not None:
+        wj = dev64(ee.jastrow_kernel.weight, device)
         keep.append(wj)
         d.use_jastrow = 1
         d.jastrow_w = ptr(wj)
     else:
         d.use_jastrow = 0
         d.jastrow_w = ptr(dd)
+    if en is not None:
+        wn = dev64(en.jastrow_kernel.weight, device)
+        at = dev64(en.atoms, device).reshape(-1)
+        keep += [wn, at]
+        d.use_jastrow_en = 1
+        d.jastrow_en_w, d.jastrow_en_atoms = ptr(wn), ptr(at)
+    else:
+        d.use_jastrow_en = 0
+        d.jastrow_en_w = d.jastrow_en_atoms = ptr(dd)
     if pool is not None:
         ct = pool.device_tables(device)
         d.det_mode = 1 if ct.explicit else 0

@@ -7,7 +7,8 @@ one-thread-per-walker kernels (``qmc_wf_psi``, ``qmc_wf_local_energy``); the
 submodules ``ao, mo, jastrow, pool, fc`` keep the reference's call signatures
 and run the staged kernels. State-dict names match the reference
 (``ao.bas_exp``, ``ao.atom_coords``, ``mo.mo_modifier``,
-``jastrow.jastrow_kernel.weight``, ``fc.weight``).
+``jastrow.jastrow_kernel.weight``, ``fc.weight``; with a list of Jastrow factors
+``jastrow.jastrow_terms.<k>.jastrow_kernel.weight``).
 """
 from __future__ import annotations
 
@@ -18,7 +19,7 @@ from torch import nn
 
 from .. import _lib
 from . import runtime as rt
-from .jastrows import JastrowFactorElectronElectron, PadeJastrowKernel
+from .jastrows import CombineJastrow, JastrowFactorElectronElectron, PadeJastrowKernel
 from .orbitals import AtomicOrbitals, MolecularOrbitals
 from .pooling import SlaterPooling
 from .tables import OrbitalConfigurations
@@ -75,7 +76,7 @@ class _PsiFunction(torch.autograd.Function):
     Gradients with respect to the electron positions are not provided."""
 
     @staticmethod
-    def forward(ctx, x, bas_exp, mo_modifier, jastrow_w, fc_weight, wf):
+    def forward(ctx, x, bas_exp, mo_modifier, jastrow_w, jastrow_en_w, fc_weight, wf):
         ctx.wf = wf
         xd = rt.dev64(x, rt.cuda_device()).reshape(-1, wf.ndim_tot)
         ctx.save_for_backward(xd)
@@ -84,11 +85,9 @@ class _PsiFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gout):
         (xd,) = ctx.saved_tensors
-        wf = ctx.wf
-        g_exp, g_mod, g_w, g_fc = wf._psi_adjoint(xd, gout.reshape(-1))
+        grads = ctx.wf._psi_adjoint(xd, gout.reshape(-1))
         need = ctx.needs_input_grad
-        return (None, g_exp if need[1] else None, g_mod if need[2] else None,
-                g_w if need[3] else None, g_fc if need[4] else None, None)
+        return (None,) + tuple(g if need[i + 1] else None for i, g in enumerate(grads)) + (None,)
 
 
 class _ElocFunction(torch.autograd.Function):
@@ -97,7 +96,7 @@ class _ElocFunction(torch.autograd.Function):
     derivatives are recomputed in the backward pass."""
 
     @staticmethod
-    def forward(ctx, x, bas_exp, mo_modifier, jastrow_w, fc_weight, wf):
+    def forward(ctx, x, bas_exp, mo_modifier, jastrow_w, jastrow_en_w, fc_weight, wf):
         ctx.wf = wf
         xd = rt.dev64(x, rt.cuda_device()).reshape(-1, wf.ndim_tot)
         ctx.save_for_backward(xd)
@@ -107,12 +106,10 @@ class _ElocFunction(torch.autograd.Function):
     @staticmethod
     def backward(ctx, gout):
         (xd,) = ctx.saved_tensors
-        wf = ctx.wf
-        g_exp, g_mod, g_w, g_fc = wf._adjoint(xd, gout.reshape(-1), "qmc_wf_local_energy_adjoint",
-                                              "qmc_eloc_adjoint_scratch_bytes")
+        grads = ctx.wf._adjoint(xd, gout.reshape(-1), "qmc_wf_local_energy_adjoint",
+                                "qmc_eloc_adjoint_scratch_bytes")
         need = ctx.needs_input_grad
-        return (None, g_exp if need[1] else None, g_mod if need[2] else None,
-                g_w if need[3] else None, g_fc if need[4] else None, None)
+        return (None,) + tuple(g if need[i + 1] else None for i, g in enumerate(grads)) + (None,)
 
 
 class SlaterJastrow(WaveFunction):
@@ -164,16 +161,19 @@ class SlaterJastrow(WaveFunction):
             self.use_jastrow = True
             if isinstance(jastrow, str) and jastrow == "default":
                 self.jastrow = JastrowFactorElectronElectron(mol, PadeJastrowKernel)
-            elif isinstance(jastrow, JastrowFactorElectronElectron):
+            elif isinstance(jastrow, list):
+                self.jastrow = CombineJastrow(jastrow)
+            elif isinstance(jastrow, nn.Module):
                 self.jastrow = jastrow
-            elif isinstance(jastrow, (list, nn.Module)):
-                raise NotImplementedError("only the Pade e-e Jastrow factor runs on the GB300 path")
             else:
                 raise TypeError("Jastrow factor not supported.")
+            rt.jastrow_parts(self.jastrow)  # the kernels' factors: Pade e-e and / or e-n
             self.jastrow_type = repr(self.jastrow)
-        for m in (self.mo, self.pool, self.jastrow):
-            if m is not None:
-                object.__setattr__(m, "_ao_module", self.ao)
+        jastrow_modules = [self.jastrow] if self.jastrow is not None else []
+        if isinstance(self.jastrow, CombineJastrow):
+            jastrow_modules += list(self.jastrow.jastrow_terms)
+        for m in [self.mo, self.pool] + jastrow_modules:
+            object.__setattr__(m, "_ao_module", self.ao)
         # kinetic energy: the Jacobi trace formula; "auto" (autograd in the
         # reference, wf_base.py:142-182) evaluates the same quantity
         self.kinetic_method = kinetic
@@ -242,8 +242,7 @@ class SlaterJastrow(WaveFunction):
             if self.use_jastrow:
                 out = self.jastrow(x) * out
             return out
-        jw = self.jastrow.jastrow_kernel.weight if self.use_jastrow else self._no_jastrow_w
-        params = (self.ao.bas_exp, self.mo.mo_modifier, jw, self.fc.weight)
+        params = self._trainable()
         if torch.is_grad_enabled() and any(p.requires_grad for p in params):
             return _PsiFunction.apply(x, *params, self)
         return self._psi(x).reshape(-1, 1).to(device=x.device, dtype=x.dtype)
@@ -264,7 +263,7 @@ class SlaterJastrow(WaveFunction):
         g = rt.dev64(gout, device)
         g_exp = torch.zeros(bt.nentries, dtype=rt.F64, device=device)
         g_W = torch.zeros((self.ao.norb, nmu), dtype=rt.F64, device=device)
-        g_w = torch.zeros(1, dtype=rt.F64, device=device)
+        g_w = torch.zeros(2, dtype=rt.F64, device=device)  # e-e and e-n Pade weights
         g_ci = torch.zeros(self.nci, dtype=rt.F64, device=device)
         scr = rt.scratch(getattr(lib, scratch_fn)(call.ref, nb), device)
         _lib.check(getattr(lib, fn)(call.ref, rt.ptr(x), nb, rt.ptr(g), rt.ptr(bt.t["w_entry"]),
@@ -275,9 +274,21 @@ class SlaterJastrow(WaveFunction):
         g_mod = torch.zeros(mod.shape, dtype=rt.F64, device=device)
         g_mod[:, :nmu] = g_W * rt.dev64(self.mo.mo_scf, device)[:, :nmu]
         cast = lambda t, p: t.to(device=p.device, dtype=p.dtype).reshape(p.shape)  # noqa: E731
-        jw = self.jastrow.jastrow_kernel.weight if self.use_jastrow else self._no_jastrow_w
-        return (cast(g_exp, self.ao.bas_exp), cast(g_mod, mod), cast(g_w, jw),
-                cast(g_ci, self.fc.weight))
+        jw, jwn = self._jastrow_weights()
+        return (cast(g_exp, self.ao.bas_exp), cast(g_mod, mod), cast(g_w[:1], jw),
+                cast(g_w[1:], jwn), cast(g_ci, self.fc.weight))
+
+    def _jastrow_weights(self):
+        """(e-e Pade weight, e-n Pade weight) parameters, a fixed placeholder for
+        an absent factor."""
+        ee, en = rt.jastrow_parts(self.jastrow if self.use_jastrow else None)
+        return (ee.jastrow_kernel.weight if ee is not None else self._no_jastrow_w,
+                en.jastrow_kernel.weight if en is not None else self._no_jastrow_w)
+
+    def _trainable(self):
+        """The parameters the hand-written adjoints differentiate."""
+        jw, jwn = self._jastrow_weights()
+        return (self.ao.bas_exp, self.mo.mo_modifier, jw, jwn, self.fc.weight)
 
     def pdf(self, pos, return_grad=False):
         """psi^2 -> (nbatch,) (wf_base.py:241-247)."""
@@ -290,8 +301,7 @@ class SlaterJastrow(WaveFunction):
         """E_L = KE + V_en + V_ee + V_nn -> (nbatch, 1) (wf_base.py:184-215).
         Differentiable with respect to ao.bas_exp, mo.mo_modifier,
         jastrow.jastrow_kernel.weight and fc.weight (hand-written adjoint)."""
-        jw = self.jastrow.jastrow_kernel.weight if self.use_jastrow else self._no_jastrow_w
-        params = (self.ao.bas_exp, self.mo.mo_modifier, jw, self.fc.weight)
+        params = self._trainable()
         if torch.is_grad_enabled() and any(p.requires_grad for p in params):
             return _ElocFunction.apply(pos, *params, self)
         el, _ = self._eloc(pos)

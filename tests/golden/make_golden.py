@@ -52,6 +52,39 @@ CASES = {
 }
 
 
+# Jastrow factors of the cases that do not use the default e-e Pade factor:
+# "ee+en" = CombineJastrow([e-e Pade, e-n Pade]) (combine_jastrow.py:7-195),
+# "en" = the e-n Pade factor alone (jastrow_factor_electron_nuclei.py:9-161),
+# with the kernels' initial weights (w of each Pade kernel).
+JASTROW = {"lih_en": ("ee+en", 1.0, 0.8), "h2o_en": ("ee+en", 1.0, 1.3),
+           "h2_en": ("en", None, 0.6), "c6h6_en": ("ee+en", 2.0, 10.0)}
+CASES.update({
+    "lih_en": ("Li 0 0 0; H 0 0 1.595", "angs", "sto-3g", "cas(2,2)", True, 12, True,
+               ("metropolis", "solver")),
+    "h2o_en": ("O 0 0 0.1173; H 0 0.7572 -0.4692; H 0 -0.7572 -0.4692", "angs", "cc-pvdz",
+               "single_double(4,4)", True, 8, True, ("metropolis", "iter", "solver")),
+    "h2_en": ("H 0 0 -0.37; H 0 0 0.37", "angs", "sto-3g", "ground_state", True, 12, False,
+              ("metropolis", "solver")),
+    "c6h6_en": (CASES["c6h6"][0], "angs", "cc-pvdz", "ground_state", True, 3, False,
+                ("iter", "oneelec")),
+})
+
+
+def make_jastrow(mol, name):
+    """The reference Jastrow object of a case (None: the default e-e factor)."""
+    if name not in JASTROW:
+        return "default"
+    from qmctorch.wavefunction.jastrows.elec_elec import JastrowFactor as JEE
+    from qmctorch.wavefunction.jastrows.elec_elec import PadeJastrowKernel as PEE
+    from qmctorch.wavefunction.jastrows.elec_nuclei import JastrowFactor as JEN
+    from qmctorch.wavefunction.jastrows.elec_nuclei import PadeJastrowKernel as PEN
+    kind, w_ee, w_en = JASTROW[name]
+    en = JEN(mol, PEN, kernel_kwargs={"w": w_en})
+    if kind == "en":
+        return en
+    return [JEE(mol, PEE, kernel_kwargs={"w": w_ee}), en]
+
+
 def seeded_positions(mol, nw, seed):
     """Electrons assigned to atoms in order of their electron count, offset by
     N(0, 1 bohr^2) per coordinate."""
@@ -84,7 +117,8 @@ def main(reference_root, only=()):
         mol.save(tmp)
         data = dict(np.load(tmp))
         os.remove(tmp)
-        wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)
+        wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo,
+                           jastrow=make_jastrow(mol, name))
         if random_ci:
             g = torch.Generator().manual_seed(7)
             wf.fc.weight.data = torch.rand(wf.fc.weight.shape, generator=g)
@@ -92,10 +126,16 @@ def main(reference_root, only=()):
         pos = torch.as_tensor(pos_np)
         data.update(case_configs=np.asarray(configs), case_include_all_mo=np.asarray(all_mo),
                     fc_weight=wf.fc.weight.detach().numpy().reshape(-1),
-                    jastrow_w=wf.jastrow.jastrow_kernel.weight.detach().numpy(),
                     pos=pos_np)
+        if name in JASTROW:
+            data.update(case_jastrow=np.asarray(JASTROW[name][0]))
+            for pname, p in wf.named_parameters():
+                if pname.startswith("jastrow."):
+                    data["param_" + pname] = p.detach().numpy().copy()
+        else:
+            data.update(jastrow_w=wf.jastrow.jastrow_kernel.weight.detach().numpy())
         with torch.no_grad():
-            if name != "c6h6":
+            if not name.startswith("c6h6"):
                 ao, dao, d2ao = wf.ao(pos, derivative=[0, 1, 2])
                 data.update(ao=ao.numpy(), dao=dao.numpy(), d2ao=d2ao.numpy(),
                             ao_sumgrad=wf.ao(pos, derivative=1).numpy(),
@@ -194,6 +234,8 @@ def main(reference_root, only=()):
             names = ["ao.bas_exp", "mo.mo_modifier", "jastrow.jastrow_kernel.weight",
                      "fc.weight"]
             params = dict(wf.named_parameters())
+            if name in JASTROW:
+                names = [n for n in params if n != "ao.atom_coords"]
             for mode in ("manual", "auto"):
                 solver.configure(grad=mode, loss="energy", track=["local_energy"])
                 solver.loss.use_weight = False

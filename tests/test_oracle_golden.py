@@ -4,14 +4,16 @@ import numpy as np
 import pytest
 
 from oracle import qmc_oracle as orc
-from tests.golden_cases import CASES, load
+from tests.golden_cases import CASES, EN_CASES, jastrow_weights, load
+
+ALL = CASES + EN_CASES
 
 RTOL = 1e-10
 
 
 def _oracle(mol, d):
     return orc.OracleSlaterJastrow(mol, configs=d["configs"], include_all_mo=d["include_all_mo"],
-                                   jastrow_w=float(d["jastrow_w"][0]), fc_weight=d["fc_weight"])
+                                   jastrow_terms=jastrow_weights(d), fc_weight=d["fc_weight"])
 
 
 def close(a, b, rtol=RTOL, atol_scale=1e-12):
@@ -21,7 +23,7 @@ def close(a, b, rtol=RTOL, atol_scale=1e-12):
     np.testing.assert_allclose(a, b, rtol=rtol, atol=atol)
 
 
-@pytest.mark.parametrize("name", CASES)
+@pytest.mark.parametrize("name", ALL)
 def test_oracle_wavefunction(name):
     mol, d = load(name)
     wf = _oracle(mol, d)
@@ -48,7 +50,7 @@ def test_oracle_wavefunction(name):
     close(wf.nuclear_repulsion(), d["v_nn"])
 
 
-@pytest.mark.parametrize("name", [c for c in CASES if "met_out" in load(c)[1]])
+@pytest.mark.parametrize("name", [c for c in ALL if "met_out" in load(c)[1]])
 def test_oracle_metropolis_replay(name):
     mol, d = load(name)
     wf = _oracle(mol, d)
@@ -57,7 +59,7 @@ def test_oracle_metropolis_replay(name):
     close(out, d["met_out"])
 
 
-@pytest.mark.parametrize("name", [c for c in CASES if "iter_out" in load(c)[1]])
+@pytest.mark.parametrize("name", [c for c in ALL if "iter_out" in load(c)[1]])
 def test_oracle_metropolis_iter_replay(name):
     mol, d = load(name)
     wf = _oracle(mol, d)
@@ -66,7 +68,7 @@ def test_oracle_metropolis_iter_replay(name):
     close(out, d["iter_out"])
 
 
-@pytest.mark.parametrize("name", [c for c in CASES if "one_out" in load(c)[1]])
+@pytest.mark.parametrize("name", [c for c in ALL if "one_out" in load(c)[1]])
 def test_oracle_metropolis_one_elec_replay(name):
     """one-elec moves: the electron index each walker moves per step was drawn
     by the reference (torch.LongTensor.random_, metropolis.py:247) and is
