@@ -543,6 +543,54 @@ def bench_serving(args):
     return out
 
 
+def _r(v, k=4):
+    return None if v is None else float("%.*g" % (k, v))
+
+
+def summarize(line, results, args, units, world, m_met, m_el, f_met, f_el):
+    """Compact record of the numbers beside the headline: the plain FP64
+    method, E_L/s, the mixed-method error on fixed positions, the C6H6,
+    serving, H_n and module-kernel figures."""
+    nw = line["config"]["nwalkers_per_gpu"]
+    out = {"fp64_walker_steps_per_s": _r(units * world / f_met),
+           "mixed_over_fp64_walker_steps": _r(f_met / m_met),
+           "el_per_s_mixed": _r(nw * args.steps * world / m_el),
+           "el_per_s_fp64": _r(nw * args.steps * world / f_el),
+           "mixed_over_fp64_el": _r(f_el / m_el),
+           "acceptance": _r(results["mixed"]["accept"], 3)}
+    p = line.get("precision_vs_fp64")
+    if p:
+        out["precision_1e5_positions"] = {"mean_eloc_diff_ha": _r(p["mean_eloc_diff_ha"], 3),
+                                          "eloc_err_p99_ha": _r(p["eloc_abs_err_p99_ha"], 3),
+                                          "psi_rel_err_median": _r(p["psi_rel_err_median"], 3)}
+    c = line.get("c6h6_single_electron")
+    if c:
+        out["c6h6_walker_sweeps_per_s"] = {"mixed": _r(c["mixed"]["walker_sweeps_per_s"]),
+                                           "fp64": _r(c["fp64"]["walker_sweeps_per_s"])}
+        out["c6h6_el_per_s"] = {"mixed": _r(c["mixed"]["el_per_s"]),
+                                "fp64": _r(c["fp64"]["el_per_s"])}
+    sv = line.get("serving")
+    if sv:
+        out["serving"] = [{"lambda": r["lambda_per_s"], "p50_s": _r(r["p50_latency_s"], 3),
+                           "p99_s": _r(r["p99_latency_s"], 3),
+                           "ws_per_s": _r(r["walker_steps_per_s"], 3),
+                           "jobs_per_launch": _r(r["jobs_per_launch"], 3)} for r in sv["rates"]]
+    h = line.get("h_n_metropolis")
+    if h:
+        ws = h["walker_steps_per_s"]
+        out["h_n_walker_steps_per_s"] = {k: _r(ws[k], 3) for k in ("H8", "H16", "H20", "H32")
+                                         if k in ws}
+    mt = line.get("mo_tensor_core")
+    if mt and "c6h6_ccpvdz" in mt:
+        out["mo_tc_c6h6"] = {"ms": _r(mt["c6h6_ccpvdz"]["ms_tc"], 3),
+                             "frac_of_hbm": _r(mt["c6h6_ccpvdz"]["frac_of_hbm"], 3)}
+    sm = line.get("small_configs")
+    if sm:
+        out["h2_single_point_s"] = _r(sm["h2_single_point"]["wall_s"], 3)
+        out["lih_epochs_per_s"] = _r(sm["lih_run"]["epochs_per_s"], 3)
+    return out
+
+
 def slowest_rank_times(torch, vals, device, world):
     """Per-quantity maximum of the ranks' timed durations (replicas: every
     rank runs its own walkers, the job takes as long as the slowest rank)."""
@@ -680,6 +728,7 @@ def run_gb300(args):
                 hbm_peak = float(json.load(f).get("hbm_gbs", hbm_peak))
         except Exception:
             pass
+        fp32_peak = peaks["fp32_gflops"]
         line = {
             "metric": METRIC,
             "value": value,
@@ -694,29 +743,24 @@ def run_gb300(args):
             "dtype": "f32+f64 (mixed)",
             "data": "synthetic (seeded walker positions; built-in cc-pVDZ tables, extended-Hueckel MOs)",
             "config": workload_config(args, nw),
-            "el_per_s": nw * args.steps * world / m_el,
-            "fp64": {"walker_steps_per_s": units * world / f_met,
-                     "el_per_s": nw * args.steps * world / f_el,
-                     "ms_per_step": f_met * 1e3 / args.steps},
-            "speedup_vs_fp64": {"walker_steps": f_met / m_met, "el": f_el / m_el},
-            "precision_vs_fp64": prec,
-            "acceptance": results["mixed"]["accept"],
-            # HBM roofline of the dominant kernel (schema): algorithmic bytes of one
-            # launch = the walkers' positions read and written once (the state stays
-            # on chip for all mc-steps); traffic = ncu DRAM bytes of one launch
-            "roofline": {"bound": "hbm", "kernel": "metropolis_kernel<float>",
-                         "achieved": hbm_alg / (m_met / args.steps) / 1e9,
-                         "peak": hbm_peak, "unit": "GB/s",
-                         "frac": hbm_alg / (m_met / args.steps) / 1e9 / hbm_peak,
-                         "traffic": TRAFFIC_PER_LAUNCH,
-                         "algorithmic_bytes_per_launch": hbm_alg,
-                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured copy)",
-                         "note": "not HBM-bound: compute / latency bound, see roofline_fp32"},
-            "roofline_fp32": {"bound": "fp32", "kernel": "metropolis_kernel<float>",
-                              "achieved": ach_m, "peak": peaks["fp32_gflops"], "unit": "GFLOP/s",
-                              "frac": ach_m / peaks["fp32_gflops"],
-                              "flops_per_walker_step": flops, "exp_per_walker_step": exps,
-                              "peak_source": "in-run FP32 FMA probe (qmc_probe_fma of measured)"},
+            # compute roofline of the dominant kernel: counted flops per walker-step
+            # (count_fp64_flops_per_psi: the work of one psi evaluation) x walker-steps
+            # per launch / the launch's CUDA-event time, against the FP32 FMA rate
+            # measured in this run; traffic = ncu DRAM bytes of one launch
+            "roofline": {"bound": "fp32", "kernel": "metropolis_kernel<float>",
+                         "achieved": ach_m / 1e3, "peak": fp32_peak / 1e3, "unit": "TFLOP/s",
+                         "frac": ach_m / fp32_peak, "traffic": TRAFFIC_PER_LAUNCH,
+                         "flops_per_walker_step": flops,
+                         "algorithmic_flops_per_launch": flops * launch_units,
+                         "launch_ms": m_met * 1e3 / args.steps,
+                         "peak_source": "FP32 FMA rate measured in this run (qmc_probe_fma; "
+                                        "MEASURED_PEAKS.json holds no FP32 figure)"},
+            "roofline_hbm": {"bound": "hbm", "kernel": "metropolis_kernel<float>",
+                             "achieved": hbm_alg / (m_met / args.steps) / 1e9,
+                             "peak": hbm_peak, "unit": "GB/s",
+                             "frac": hbm_alg / (m_met / args.steps) / 1e9 / hbm_peak,
+                             "algorithmic_bytes_per_launch": hbm_alg,
+                             "note": "positions in and out once per launch: not HBM-bound"},
             "roofline_fp64": {"bound": "fp64", "kernel": "metropolis_kernel<double>",
                               "achieved": ach_f, "peak": peaks["fp64_gflops"], "unit": "GFLOP/s",
                               "frac": ach_f / peaks["fp64_gflops"]},
@@ -732,9 +776,13 @@ def run_gb300(args):
             "module_kernels": staged,
             "mo_tensor_core": mo_tc,
             "h_n_metropolis": h_n,
+            "precision_vs_fp64": prec,
             "gpu_launches": 4 * args.steps,
             "clocks": clk,
         }
+        # the headline's companions, last on the line so that a tail of the
+        # output carries them
+        line["summary"] = summarize(line, results, args, units, world, m_met, m_el, f_met, f_el)
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

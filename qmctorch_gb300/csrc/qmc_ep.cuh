@@ -480,6 +480,139 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
 // ---------------------------------------------------------------------------
 // phases 2 and 3
 // ---------------------------------------------------------------------------
+// psi / Metropolis determinant phase of one (walker, spin) channel in
+// excitation mode for n = N <= 8 occupied and nv <= kRegNV virtual columns:
+// the spin's MO rows are loaded into registers once, factored (LU with partial
+// pivoting) and A^-1 A_virt solved there -- the operations of lu_factor and
+// lu_solve in the same order, so bitwise the same values -- and only
+// A^-1 A_virt is written back (in place over the virtual columns) for the
+// excitation determinants. Returns det(A) in FP64 (product of the pivots).
+constexpr int kRegNV = 2;
+// largest n of the register path: 5 under the 64-register bound of the FP32
+// kernels (more spills), 6 for FP64 (128 registers)
+template <typename R>
+constexpr int kRegMaxN = kMixed<R> ? 5 : 6;
+
+template <typename R, int N>
+__device__ inline double lu_solve_regs(R* rows, int64_t rs, int64_t cs, int nv) {
+  constexpr int NC = N + kRegNV;
+  R a[N][NC];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < NC; ++j) a[i][j] = (j < N + nv) ? rows[i * rs + j * cs] : (R)0;
+  double det = 1.0;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    int p = k;
+    R amax = fabs(a[k][k]);
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const R v = fabs(a[i][k]);
+      if (v > amax) {
+        amax = v;
+        p = i;
+      }
+    }
+    // row interchange: the occupied columns as lu_factor does at this step,
+    // the virtual columns as lu_solve's pivot pass does afterwards (the same
+    // transpositions in the same order)
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const bool sw = (i == p);
+#pragma unroll
+      for (int j = 0; j < NC; ++j) {
+        const R x = a[k][j], y = a[i][j];
+        a[k][j] = sw ? y : x;
+        a[i][j] = sw ? x : y;
+      }
+    }
+    if (p != k) det = -det;
+    const R akk = a[k][k];
+    det *= (double)akk;
+    const R inv = akk != (R)0 ? (R)1 / akk : (R)0;
+    a[k][k] = inv;
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const R l = a[i][k] * inv;
+      a[i][k] = l;
+#pragma unroll
+      for (int j = k + 1; j < N; ++j) a[i][j] = fma(-l, a[k][j], a[i][j]);
+    }
+  }
+#pragma unroll
+  for (int c = 0; c < kRegNV; ++c) {
+    if (c >= nv) break;
+    const int j = N + c;
+#pragma unroll
+    for (int i = 1; i < N; ++i) {
+      R s = a[i][j];
+#pragma unroll
+      for (int k = 0; k < i; ++k) s = fma(-a[i][k], a[k][j], s);
+      a[i][j] = s;
+    }
+#pragma unroll
+    for (int i = N - 1; i >= 0; --i) {
+      R s = a[i][j];
+#pragma unroll
+      for (int k = i + 1; k < N; ++k) s = fma(-a[i][k], a[k][j], s);
+      a[i][j] = s * a[i][i];
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) rows[i * rs + j * cs] = a[i][j];
+  }
+  return det;
+}
+
+// Dispatch of lu_solve_regs on n; false when n or nv is beyond the register path.
+template <typename R>
+__device__ inline bool lu_solve_regs_n(R* rows, int64_t rs, int64_t cs, int n, int nv,
+                                       double* det) {
+  if (nv > kRegNV || n > kRegMaxN<R>) return false;
+  switch (n) {
+    case 1: *det = lu_solve_regs<R, 1>(rows, rs, cs, nv); return true;
+    case 2: *det = lu_solve_regs<R, 2>(rows, rs, cs, nv); return true;
+    case 3: *det = lu_solve_regs<R, 3>(rows, rs, cs, nv); return true;
+    case 4: *det = lu_solve_regs<R, 4>(rows, rs, cs, nv); return true;
+    case 5: *det = lu_solve_regs<R, 5>(rows, rs, cs, nv); return true;
+    default: break;
+  }
+  if constexpr (kRegMaxN<R> >= 6) {
+    switch (n) {
+      case 6: *det = lu_solve_regs<R, 6>(rows, rs, cs, nv); return true;
+
+
+      default: break;
+    }
+  }
+  return false;
+}
+
+// Excitation determinant values relative to det(A) (det_unique_single_double,
+// slater_pooling.py:147-260) from X = A^-1 A_virt: 1 (ground state), X_ij
+// (single), det of the 2 x 2 block of X (double).
+template <typename R, typename T>
+__device__ inline void excitation_values(const qmc_wf_desc& d, int spin, CView<R> X, int nv,
+                                         T* dv, int64_t s) {
+  const int nd = d.ndet[spin];
+  const int* tab = d.det_table[spin];
+  for (int u = 0; u < nd; ++u) {
+    const int ord = __ldg(tab + 5 * u);
+    R v = (R)1;
+    if (ord == 1) {
+      const int i0 = __ldg(tab + 5 * u + 1);
+      v = X(i0 / nv, i0 % nv);
+    } else if (ord >= 2) {
+      const int i0 = __ldg(tab + 5 * u + 1), i1 = __ldg(tab + 5 * u + 2);
+      const int i2 = __ldg(tab + 5 * u + 3), i3 = __ldg(tab + 5 * u + 4);
+      const R t00 = X(i0 / nv, i0 % nv), t01 = X(i1 / nv, i1 % nv);
+      const R t10 = X(i2 / nv, i2 % nv), t11 = X(i3 / nv, i3 % nv);
+      v = t00 * t11 - t01 * t10;
+    }
+    dv[u * s] = (T)v;
+  }
+}
+
 template <typename R, bool OP>
 __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned char* scr,
                               int64_t ss, int64_t w, int spin, R* mo_s, const R* bk_s, int wl,
@@ -497,16 +630,23 @@ __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned 
   wk.rc = MView<R>{rptr<R>(scr, L.rc[spin], ss, w), ss, ss};
   wk.X64 = MView<double>{rptr<double>(scr, L.x64[spin], ss, w), vm * ss, ss};
   wk.Y64 = MView<double>{rptr<double>(scr, L.y64[spin], ss, w), (int64_t)L.omax * ss, ss};
+  T* dv = rptr<T>(scr, L.dv, ss, w) + (spin ? d.ndet[0] * ss : 0);
   if (!OP && d.det_mode == QMC_DET_EXCITATION) {
     // in place (the MO rows are recomputed before every evaluation): the LU of
     // the occupied columns and A^-1 A_virt over the virtual columns of the
     // spin's MO rows, the same operations in the same order as on copies
     R* rows = mo_s + row0 * rs + wl;
     const int n = spin ? d.ndown : d.nup;
+    const int nv = d.max_orb[spin] - n;
+    double det;
+    if (n > 0 && lu_solve_regs_n<R>(rows, rs, cs, n, nv, &det)) {
+      dref[spin * nwb + wl] = det;
+      excitation_values<R, T>(d, spin, CView<R>{rows + n * cs, rs, cs}, nv > 0 ? nv : 1, dv, ss);
+      return;
+    }
     wk.LU = MView<R>{rows, rs, cs};
     wk.X = MView<R>{rows + n * cs, rs, cs};
   }
-  T* dv = rptr<T>(scr, L.dv, ss, w) + (spin ? d.ndet[0] * ss : 0);
   double* ov = OP ? rptr<double>(scr, L.ov, ss, w) + (spin ? d.ndet[0] * ss : 0) : nullptr;
   spin_channel<R, OP, T>(d, spin, mo, bk, wk, SpinOut<T>{dv, ov, ss, &dref[spin * nwb + wl]});
 }
