@@ -381,8 +381,55 @@ def make_metropolis_generic(reference_root):
     print("wrote", out_file, os.path.getsize(out_file), "bytes")
 
 
+# Chains of the reference HMC sampler (hamiltonian.py:10-201): on the analytic
+# density of the drift-diffusion fixture, and on the H2 sto-3g SlaterJastrow of
+# the "h2" case (forces by the reference's autograd through the density).
+HMC = {"nwalkers": 16, "nelec": 2, "ndim": 3, "nstep": 12, "step_size": 0.1, "L": 6,
+       "ntherm": -6, "ndecor": 2, "seed": 777}
+
+
+def make_hamiltonian(reference_root):
+    ref_stubs.install(reference_root)
+    import torch
+    from qmctorch.sampler.hamiltonian import Hamiltonian
+    from qmctorch.utils import set_torch_double_precision
+    from qmctorch.wavefunction import SlaterJastrow
+    from qmctorch_gb300.scf import Molecule
+
+    set_torch_double_precision()
+    a, c = gmet_density_params()
+    at, ct = torch.as_tensor(a), torch.as_tensor(c)
+
+    def pdf(x):
+        return torch.exp(-(at * (x - ct) ** 2).sum(-1))
+
+    g = HMC
+    pos0 = np.random.default_rng(9).normal(size=(g["nwalkers"], g["nelec"] * g["ndim"]))
+
+    def sampler():
+        return Hamiltonian(nwalkers=g["nwalkers"], nstep=g["nstep"], step_size=g["step_size"],
+                           L=g["L"], ntherm=g["ntherm"], ndecor=g["ndecor"], nelec=g["nelec"],
+                           ndim=g["ndim"], init={"method": "uniform", "min": -1, "max": 1})
+    s = sampler()
+    torch.manual_seed(g["seed"])
+    samples = s(pdf, pos=torch.as_tensor(pos0), with_tqdm=False)
+    atoms, unit, basis, configs, all_mo = CASES["h2"][:5]
+    torch.manual_seed(1234)
+    mol = Molecule(atoms, unit=unit, basis=basis)
+    wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)
+    h2pos0 = seeded_positions(mol, g["nwalkers"], seed=31)
+    s2 = sampler()
+    torch.manual_seed(g["seed"] + 1)
+    h2samples = s2(wf.pdf, pos=torch.as_tensor(h2pos0), with_tqdm=False)
+    out_file = os.path.join(HERE, "hamiltonian.npz")
+    np.savez_compressed(out_file, pos0=pos0, samples=samples.detach().numpy(),
+                        h2_pos0=h2pos0, h2_samples=h2samples.detach().numpy(),
+                        **{"cfg_" + k: np.asarray(v) for k, v in HMC.items()})
+    print("wrote", out_file, os.path.getsize(out_file), "bytes")
+
+
 EXTRA = {"gmetropolis": "make_gmetropolis", "walkers": "make_walkers",
-         "metropolis_generic": "make_metropolis_generic"}
+         "metropolis_generic": "make_metropolis_generic", "hamiltonian": "make_hamiltonian"}
 
 
 if __name__ == "__main__":

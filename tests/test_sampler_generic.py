@@ -95,3 +95,27 @@ def test_replay_needs_a_wave_function():
     s = Metropolis(nwalkers=4, nstep=2, nelec=2, init={"method": "uniform", "min": -1, "max": 1})
     with pytest.raises(ValueError):
         s(pdf, pos=torch.zeros(4, 6, dtype=torch.float64), replay={"proposals": None})
+
+
+HMC = {"nwalkers": 16, "nelec": 2, "ndim": 3, "nstep": 12, "step_size": 0.1, "L": 6,
+       "ntherm": -6, "ndecor": 2, "seed": 777}
+
+
+def _hmc():
+    from qmctorch_gb300.sampler import Hamiltonian
+    g = HMC
+    return Hamiltonian(nwalkers=g["nwalkers"], nstep=g["nstep"], step_size=g["step_size"],
+                       L=g["L"], ntherm=g["ntherm"], ndecor=g["ndecor"], nelec=g["nelec"],
+                       ndim=g["ndim"], init={"method": "uniform", "min": -1, "max": 1})
+
+
+def test_hamiltonian_on_arbitrary_density_matches_reference():
+    """HMC (hamiltonian.py:10-201) with autograd forces on the analytic
+    density: the reference's chain to 1e-13."""
+    torch.set_default_dtype(torch.float64)
+    gold = _gold("hamiltonian")
+    pdf, _, _ = _density()
+    s = _hmc()
+    torch.manual_seed(HMC["seed"])
+    samples = s(pdf, pos=torch.as_tensor(gold["pos0"]), with_tqdm=False)
+    np.testing.assert_allclose(samples.detach().numpy(), gold["samples"], rtol=0, atol=1e-13)
