@@ -46,6 +46,10 @@ class OracleBasis:
             df = np.array([DF[int(2 * v - 1)] for v in kd], dtype=np.float64)
             norm = norm * (4.0 * a) ** (kd / 2.0) / np.sqrt(df)
         self.norm_cst = norm
+        # index_add of the contraction (atomic_orbitals.py:654-669) as a
+        # (primitive x AO) matrix of the bas_coeffs
+        self.contraction = np.zeros((len(self.index_ctr), self.nao))
+        self.contraction[np.arange(len(self.index_ctr)), self.index_ctr] = self.bas_coeffs
 
 
 def _fast_power(x, k):
@@ -81,59 +85,63 @@ def ao_values(b: OracleBasis, pos, derivative=0, sum_grad=True):
     # radial_gaussian_pure
     R2 = r * r
     er = np.exp(-alpha * R2)
-    bexp_er = alpha * er
-    nabla_er = -2.0 * bexp_er[..., None] * xyz          # (nb,ne,np,3)
-    lap_er = alpha * er * (4.0 * alpha * R2 - 6.0)      # sum_hess
     # cartesian harmonics
     k = b.k
     xyz_k = _fast_power(xyz, k)
     Y = xyz_k.prod(-1)
-    km1 = np.maximum(k - 1, 0)
-    km2 = np.maximum(k - 2, 0)
-    xyz_km1 = _fast_power(xyz, km1)
-    xyz_km2 = _fast_power(xyz, km2)
-    kx, ky, kz = k[:, 0], k[:, 1], k[:, 2]
-    dY = np.stack((kx * xyz_km1[..., 0] * xyz_k[..., 1] * xyz_k[..., 2],
-                   ky * xyz_k[..., 0] * xyz_km1[..., 1] * xyz_k[..., 2],
-                   kz * xyz_k[..., 0] * xyz_k[..., 1] * xyz_km1[..., 2]), axis=-1)
-    d2Y = (kx * (kx - 1) * xyz_km2[..., 0] * xyz_k[..., 1] * xyz_k[..., 2]
-           + ky * (ky - 1) * xyz_k[..., 0] * xyz_km2[..., 1] * xyz_k[..., 2]
-           + kz * (kz - 1) * xyz_k[..., 0] * xyz_k[..., 1] * xyz_km2[..., 2])
     nc = b.norm_cst
     cc = b.bas_coeffs
     idx = b.index_ctr
 
+    def derivs():  # radial and harmonic derivative pieces (only when asked for)
+        bexp_er = alpha * er
+        nabla_er = -2.0 * bexp_er[..., None] * xyz          # (nb,ne,np,3)
+        lap_er = alpha * er * (4.0 * alpha * R2 - 6.0)      # sum_hess
+        km1 = np.maximum(k - 1, 0)
+        km2 = np.maximum(k - 2, 0)
+        xyz_km1 = _fast_power(xyz, km1)
+        xyz_km2 = _fast_power(xyz, km2)
+        kx, ky, kz = k[:, 0], k[:, 1], k[:, 2]
+        dY = np.stack((kx * xyz_km1[..., 0] * xyz_k[..., 1] * xyz_k[..., 2],
+                       ky * xyz_k[..., 0] * xyz_km1[..., 1] * xyz_k[..., 2],
+                       kz * xyz_k[..., 0] * xyz_k[..., 1] * xyz_km1[..., 2]), axis=-1)
+        d2Y = (kx * (kx - 1) * xyz_km2[..., 0] * xyz_k[..., 1] * xyz_k[..., 2]
+               + ky * (ky - 1) * xyz_k[..., 0] * xyz_km2[..., 1] * xyz_k[..., 2]
+               + kz * (kz - 1) * xyz_k[..., 0] * xyz_k[..., 1] * xyz_km2[..., 2])
+        return nabla_er, lap_er, dY, d2Y
+
     def contract(v):  # _contract 654-669 (value path applies coeffs only here)
         if b.contract:
-            return _index_add(nb, ne, b.nao, idx, cc * v)
+            return v @ b.contraction
         return v
 
     def ao_kernel():  # _ao_kernel 236-249
         return contract(nc * er * Y)
 
-    def grad_kernel():  # _gradient_kernel 330-356
+    def grad_kernel(nabla_er, dY):  # _gradient_kernel 330-356
         bas = nabla_er * Y[..., None] + er[..., None] * dY
         bas = nc[:, None] * cc[:, None] * bas
         if b.contract:
             return _index_add(nb, ne, b.nao, idx, bas, extra=(3,))
         return bas
 
-    def sum_grad_kernel():  # _sum_gradient_kernel 290-307
+    def sum_grad_kernel(nabla_er, dY):  # _sum_gradient_kernel 290-307
         dR = nabla_er.sum(3)
         dYs = dY.sum(-1)
         return contract(nc * (dR * Y + er * dYs))
 
-    def lap_kernel():  # _sum_diag_hessian_kernel 397-423
+    def lap_kernel(nabla_er, lap_er, dY, d2Y):  # _sum_diag_hessian_kernel 397-423
         return contract(nc * (lap_er * Y + 2.0 * (nabla_er * dY).sum(3) + er * d2Y))
 
     if derivative == 0 or derivative == [0]:
         return ao_kernel()
+    nabla_er, lap_er, dY, d2Y = derivs()
     if derivative == 1 or derivative == [1]:
-        return sum_grad_kernel() if sum_grad else grad_kernel()
+        return sum_grad_kernel(nabla_er, dY) if sum_grad else grad_kernel(nabla_er, dY)
     if derivative == 2 or derivative == [2]:
-        return lap_kernel()
+        return lap_kernel(nabla_er, lap_er, dY, d2Y)
     if list(derivative) == [0, 1, 2]:
-        return ao_kernel(), grad_kernel(), lap_kernel()
+        return ao_kernel(), grad_kernel(nabla_er, dY), lap_kernel(nabla_er, lap_er, dY, d2Y)
     raise ValueError("derivative must be 0, 1, 2 or [0, 1, 2]")
 
 
