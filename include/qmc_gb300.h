@@ -362,10 +362,13 @@ int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a,
  * (no reference counterpart: the serving loop's continuous batching). Job j
  * is (descs[j], args[j]) with its own scratch[j] of scratch_bytes[j] bytes;
  * each job's walkers evolve exactly as in a qmc_metropolis_run call with the
- * same arguments (bitwise), whatever the other jobs are. Jobs must share the
- * launch shape: precision, electron count, determinant columns and table
- * sizes (e.g. H_n chains of one n); otherwise QMC_ERR_SHAPE. All-electron
- * moves without replay inputs or psi_out only (QMC_ERR_UNSUPPORTED).
+ * same arguments (bitwise), whatever the other jobs are. Jobs may differ in
+ * molecule, electron count, basis and CI expansion; they must share the
+ * precision and the MO column class of the determinants (nmo_used <= 8,
+ * 9..16 or 17..24); otherwise QMC_ERR_SHAPE. Each job runs the launch plan it
+ * would get alone; the block size and shared memory are the largest over the
+ * jobs. All-electron moves without replay inputs or psi_out only
+ * (QMC_ERR_UNSUPPORTED).
  */
 #define QMC_MAX_BATCH 32
 int qmc_metropolis_run_batch(const qmc_wf_desc* descs, const qmc_metropolis_args* args,

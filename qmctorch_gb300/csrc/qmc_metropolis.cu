@@ -28,6 +28,9 @@ using namespace qmc;
 int qmc_sweep_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void* stream);
 bool qmc_sweep_eligible(const qmc_wf_desc* d, const qmc_metropolis_args* a);
 
+// column-chunk class of the electron-parallel kernels (JC = 8, 16, 24)
+static inline int mo_chunk_class(int nmo_used) { return nmo_used <= 8 ? 0 : (nmo_used <= 16 ? 1 : 2); }
+
 extern "C" {
 
 int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void* scratch,
@@ -73,8 +76,8 @@ int qmc_metropolis_run_batch(const qmc_wf_desc* descs, const qmc_metropolis_args
     if (a->nwalkers > 0 && (!a->pos || !scratch[j])) return QMC_ERR_ARG;
     if (a->samples && a->nsnap < 0) return QMC_ERR_ARG;
     if (scratch_bytes[j] < qmc_metropolis_scratch_bytes(d, a->nwalkers)) return QMC_ERR_SCRATCH;
-    if (d->precision != descs[0].precision || d->nelec != descs[0].nelec ||
-        d->nmo_used != descs[0].nmo_used)
+    if (d->precision != descs[0].precision ||
+        mo_chunk_class(d->nmo_used) != mo_chunk_class(descs[0].nmo_used))
       return QMC_ERR_SHAPE;
   }
   cudaStream_t s = (cudaStream_t)stream;

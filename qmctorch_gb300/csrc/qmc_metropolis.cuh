@@ -155,62 +155,66 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads)
   metropolis_block<R, JC>(d, a, scr, ss, S, blockIdx.x, smem);
 }
 
-// Several independent jobs (molecules of one launch shape: same electron
-// count and table sizes) in one launch. The job table travels in the kernel
-// parameters; block b serves job j with block0[j] <= b < block0[j + 1].
+// Several independent jobs in one launch: molecules of any size whose MO
+// column count falls in this kernel's chunk class (JC), in one precision. The
+// job table travels in the kernel parameters with each job's own launch plan
+// (walkers per block, electron slots, shared-memory offsets: the plan the job
+// would get alone); block b serves job j with block0[j] <= b < block0[j + 1].
+// The block size and the dynamic shared memory are the largest over the jobs;
+// threads past a job's plan idle through its barriers.
 struct MetBatchJob {
   qmc_wf_desc d;
   qmc_metropolis_args a;
   unsigned char* scr;
   int64_t ss;
+  EPShape S;
 };
 struct MetBatch {
   int32_t njobs;
   int64_t block0[QMC_MAX_BATCH + 1];
   MetBatchJob job[QMC_MAX_BATCH];
 };
+static_assert(sizeof(MetBatch) <= 32000, "kernel parameter block above the 32 KB limit");
 
 template <typename R, int JC>
 __global__ void __launch_bounds__(EPBound<R>::kThreads)
-    metropolis_batch_kernel(const __grid_constant__ MetBatch b, const __grid_constant__ EPShape S) {
+    metropolis_batch_kernel(const __grid_constant__ MetBatch b) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int64_t bid = blockIdx.x;
   int j = 0;
   while (j + 1 < b.njobs && b.block0[j + 1] <= bid) ++j;
   const MetBatchJob& J = b.job[j];
-  metropolis_block<R, JC>(J.d, J.a, J.scr, J.ss, S, bid - b.block0[j], smem);
+  metropolis_block<R, JC>(J.d, J.a, J.scr, J.ss, J.S, bid - b.block0[j], smem);
 }
 
 template <typename R, int JC>
 int launch_metropolis_batch(const qmc_wf_desc* descs, const qmc_metropolis_args* args,
-                                   void* const* scratch, int njobs, cudaStream_t s) {
-  int64_t nwt = 0;
-  for (int j = 0; j < njobs; ++j) nwt += args[j].nwalkers;
-  const EPShape S = ep_plan<R>(descs[0], 2, JC, metropolis_batch_kernel<R, JC>, nwt);
-  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
-  for (int j = 1; j < njobs; ++j) {
-    const EPShape Sj = ep_shape<R>(descs[j], 2, S.nwb, JC, S.nslot);
-    if (Sj.smem != S.smem || Sj.o_pos != S.o_pos || Sj.o_mo != S.o_mo || Sj.o_acc != S.o_acc ||
-        Sj.pstride != S.pstride ||
-        Sj.ncol != S.ncol || Sj.nthreads != S.nthreads)
-      return QMC_ERR_SHAPE;
-  }
-  int st = prepare_smem(metropolis_batch_kernel<R, JC>, S.smem);
-  if (st) return st;
+                            void* const* scratch, int njobs, cudaStream_t s) {
   static MetBatch b;  // host staging of the parameter block (copied at launch)
   static std::mutex mu;
   std::lock_guard<std::mutex> g(mu);
+  int64_t smem = 0;
+  int nthreads = 32;
   b.njobs = njobs;
   b.block0[0] = 0;
   for (int j = 0; j < njobs; ++j) {
+    const int64_t nw = args[j].nwalkers > 0 ? args[j].nwalkers : 1;
+    const EPShape S = ep_plan<R>(descs[j], 2, JC, metropolis_batch_kernel<R, JC>, nw);
+    if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads)
+      return QMC_ERR_SHAPE;
+    if (S.smem > smem) smem = S.smem;
+    if (S.nthreads > nthreads) nthreads = S.nthreads;
     b.job[j].d = descs[j];
     b.job[j].a = args[j];
     b.job[j].scr = (unsigned char*)scratch[j];
     b.job[j].ss = pad_walkers(args[j].nwalkers);
+    b.job[j].S = S;
     b.block0[j + 1] = b.block0[j] + (args[j].nwalkers + S.nwb - 1) / S.nwb;
   }
   if (b.block0[njobs] == 0) return QMC_OK;
-  metropolis_batch_kernel<R, JC><<<(unsigned)b.block0[njobs], S.nthreads, S.smem, s>>>(b, S);
+  int st = prepare_smem(metropolis_batch_kernel<R, JC>, smem);
+  if (st) return st;
+  metropolis_batch_kernel<R, JC><<<(unsigned)b.block0[njobs], nthreads, smem, s>>>(b);
   return launch_status();
 }
 

@@ -25,7 +25,8 @@ Scheduling (``Scheduler``):
   retires;
 * the sampling work is cut into slices of ``slice_steps`` steps. Each
   scheduler pass gathers the jobs whose previous slice has finished, groups
-  them by launch shape (electron count, table sizes, precision) and issues
+  them by launch class (precision and MO column class; molecules of any size
+  share a launch, each block running its job's own plan) and issues
   one ``qmc_metropolis_run_batch`` launch per group of up to ``QMC_MAX_BATCH``
   jobs, on a pool of CUDA streams, so groups overlap on the device and a job
   admitted while others run joins the next launch of its group;
@@ -281,6 +282,13 @@ class GPUExecutor:
         return (mol.nelec, mol.nup, mol.basis.nao, len(mol.atoms), req.basis, req.configs,
                 req.precision)
 
+    @staticmethod
+    def _launch_key(wf):
+        """Jobs that can share one qmc_metropolis_run_batch launch: the same
+        precision and MO column class of the determinants (any molecule)."""
+        n = wf.highest_occ_mo
+        return (wf.precision, 0 if n <= 8 else (1 if n <= 16 else 2))
+
     def footprint(self, req):
         mol = self._molecule(req)
         k = self._shape_key(req, mol)
@@ -323,7 +331,7 @@ class GPUExecutor:
         # positions are written on the default stream; the pool streams wait for them
         h["ready"] = torch.cuda.Event()
         h["ready"].record(torch.cuda.current_stream(self.device))
-        return h, self._shape_key(req, mol)
+        return h, self._launch_key(wf)
 
     def _args(self, h, offset, nstep):
         a = self._lib.MetropolisArgs()

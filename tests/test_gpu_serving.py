@@ -2,7 +2,8 @@
 compensated statistics kernel and the continuous-batching server.
 
 * qmc_metropolis_run_batch advances every job bitwise as qmc_metropolis_run
-  does alone; jobs of different launch shapes are refused (QMC_ERR_SHAPE).
+  does alone, with molecules of different sizes in one launch; jobs of
+  different precisions are refused (QMC_ERR_SHAPE).
 * qmc_reduce_stats: mean within 1e-15 and variance within 1e-13 relative of an
   exactly rounded reference (math.fsum), n = 1 gives a NaN variance as
   torch.var does.
@@ -46,7 +47,9 @@ def test_batch_launch_matches_single_launches(precision):
     from qmctorch_gb300 import _lib
     from qmctorch_gb300.serving import seeded_positions
     lib = _lib.lib()
-    jobs = [(_mol(4, 0.74), 700, 11), (_mol(4, 0.95), 1500, 12), (_mol(4, 1.2), 33, 13)]
+    # molecules of different sizes share the launch (one MO column class)
+    jobs = [(_mol(4, 0.74), 700, 11), (_mol(10, 0.95), 1500, 12), (_mol(6, 1.2), 33, 13),
+            (_mol(16, 0.9), 257, 14)]
     wfs = [_wf(m, precision) for m, _, _ in jobs]
     x0 = [torch.as_tensor(seeded_positions(m, nw, s), device="cuda") for m, nw, s in jobs]
     # alone
@@ -74,8 +77,8 @@ def test_batch_launch_matches_single_launches(precision):
     torch.cuda.synchronize()
     for xa, xb in zip(alone, xs):
         assert torch.equal(xa, xb)
-    # different launch shapes are refused
-    other = _wf(_mol(6, 0.74), precision)
+    # a job of another precision is refused
+    other = _wf(_mol(6, 0.74), "fp64" if precision == "mixed" else "mixed")
     c6 = other._desc(torch.device("cuda"))
     x6 = torch.as_tensor(seeded_positions(other.mol, 64, 1), device="cuda")
     s6 = torch.empty(lib.qmc_metropolis_scratch_bytes(c6.ref, 64), dtype=torch.uint8, device="cuda")
@@ -139,7 +142,7 @@ def test_result_is_the_same_alone_and_in_the_mix():
     for r in reqs[4:]:  # arrive while the first ones run
         srv.submit(copy.copy(r))
     srv.run()
-    assert srv.launches > len(reqs)
+    assert srv.launched_jobs > srv.launches  # requests of different sizes shared launches
     for rid, r in enumerate(reqs):
         mixed = srv.results[rid]
         alone = single_point(copy.copy(r))
