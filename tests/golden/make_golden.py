@@ -428,7 +428,55 @@ def make_hamiltonian(reference_root):
     print("wrote", out_file, os.path.getsize(out_file), "bytes")
 
 
-EXTRA = {"gmetropolis": "make_gmetropolis", "walkers": "make_walkers",
+# The reference's single-precision run (set_torch_single_precision,
+# utils/torch_utils.py:16-21) of the LiH cas(2,2) case: psi, E_L and the
+# manual / automatic parameter gradients of its FP32 autograd.
+def make_fp32(reference_root):
+    ref_stubs.install(reference_root)
+    import torch
+    from qmctorch.sampler import Metropolis
+    from qmctorch.solver import Solver
+    from qmctorch.utils.torch_utils import set_torch_single_precision
+    from qmctorch.wavefunction import SlaterJastrow
+    from qmctorch_gb300.scf import Molecule
+
+    atoms, unit, basis, configs, all_mo, nw = CASES["lih_cas"][:6]
+    torch.manual_seed(1234)
+    mol = Molecule(atoms, unit=unit, basis=basis)
+    set_torch_single_precision()
+    try:
+        wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)
+        g = torch.Generator().manual_seed(7)
+        wf.fc.weight.data = torch.rand(wf.fc.weight.shape, generator=g).float()
+        pos = torch.as_tensor(seeded_positions(mol, nw, seed=11), dtype=torch.float32)
+        data = {"pos32": pos.numpy(), "fc_weight32": wf.fc.weight.detach().numpy().reshape(-1)}
+        with torch.no_grad():
+            data.update(psi32=wf(pos).numpy(), eloc32=wf.local_energy(pos).numpy())
+        sampler = Metropolis(nwalkers=nw, nstep=2, step_size=0.2, nelec=mol.nelec,
+                             init=mol.domain("atomic"))
+        opt = torch.optim.Adam(wf.parameters(), lr=1e-3)
+        solver = Solver(wf=wf, sampler=sampler, optimizer=opt, output="_unused.hdf5")
+        names = ["ao.bas_exp", "mo.mo_modifier", "jastrow.jastrow_kernel.weight", "fc.weight"]
+        params = dict(wf.named_parameters())
+        for mode in ("manual", "auto"):
+            solver.configure(grad=mode, loss="energy", track=["local_energy"])
+            solver.loss.use_weight = False
+            opt.zero_grad()
+            wf.zero_grad()
+            loss, _ = solver.evaluate_gradient(pos.clone().requires_grad_(mode == "auto"))
+            data["grad32_%s_loss" % mode] = np.asarray(float(loss))
+            for n in names:
+                gr = params[n].grad
+                data["grad32_%s_%s" % (mode, n)] = (np.zeros(params[n].shape) if gr is None
+                                                    else gr.detach().numpy().copy())
+    finally:
+        torch.set_default_dtype(torch.float64)
+    out_file = os.path.join(HERE, "lih_cas_fp32.npz")
+    np.savez_compressed(out_file, **data)
+    print("wrote", out_file, os.path.getsize(out_file), "bytes")
+
+
+EXTRA = {"gmetropolis": "make_gmetropolis", "walkers": "make_walkers", "fp32": "make_fp32",
          "metropolis_generic": "make_metropolis_generic", "hamiltonian": "make_hamiltonian"}
 
 

@@ -180,3 +180,45 @@ def test_gradients_are_bitwise_reproducible():
             grads.append([params[n].grad.detach().clone() for n in PARAMS])
         for a, b in zip(*grads):
             assert torch.equal(a, b)
+
+
+@pytest.mark.parametrize("mode", ["manual", "auto"])
+def test_single_precision_arm_matches_reference_fp32_autograd(mode):
+    """The LiH cas(2,2) configuration in single precision: the reference run
+    with torch's default dtype float32 (set_torch_single_precision,
+    utils/torch_utils.py:16-21) against this package's mixed method on the
+    same FP32 positions and CI weights. The reference's FP32 autograd itself
+    differs from its FP64 run by ~1e-6 of the largest gradient; the bar is
+    1e-4 of the largest gradient, and 1e-5 relative on the loss (the mixed
+    local energies are within 5e-3 Ha per walker, their mean far closer)."""
+    import os
+
+    from qmctorch_gb300.sampler import Metropolis
+    from qmctorch_gb300.solver import Solver
+    from tests.golden_cases import GOLDEN
+    with np.load(os.path.join(GOLDEN, "lih_cas_fp32.npz")) as f:
+        g32 = {k: f[k] for k in f.files}
+    mol, d = load("lih_cas")
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    torch.set_default_dtype(torch.float64)
+    wf = SlaterJastrow(mol, configs=d["configs"], include_all_mo=d["include_all_mo"], cuda=True,
+                       precision="mixed")
+    wf.fc.weight.data = torch.as_tensor(g32["fc_weight32"].astype(np.float64),
+                                        device="cuda").reshape(1, -1)
+    pos = torch.as_tensor(g32["pos32"].astype(np.float64), device="cuda")
+    sampler = Metropolis(nwalkers=len(pos), nstep=2, step_size=0.2, nelec=mol.nelec,
+                         init=mol.domain("atomic"), cuda=True)
+    opt = torch.optim.Adam(wf.parameters(), lr=1e-3)
+    solver = Solver(wf=wf, sampler=sampler, optimizer=opt)
+    solver.configure(grad=mode, loss="energy", track=["local_energy"])
+    solver.loss.use_weight = False
+    opt.zero_grad()
+    loss, _ = solver.evaluate_gradient(pos)
+    ref_loss = float(g32["grad32_%s_loss" % mode])
+    assert abs(float(loss.detach()) - ref_loss) < 1e-5 * abs(ref_loss)
+    params = dict(wf.named_parameters())
+    scale = max(np.abs(g32["grad32_%s_%s" % (mode, n)]).max() for n in PARAMS)
+    for n in PARAMS:
+        ref = g32["grad32_%s_%s" % (mode, n)]
+        got = params[n].grad.detach().cpu().numpy().reshape(ref.shape)
+        np.testing.assert_allclose(got, ref, rtol=0, atol=1e-4 * scale, err_msg=n)
