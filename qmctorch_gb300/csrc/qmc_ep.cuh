@@ -489,9 +489,11 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
 // excitation determinants. Returns det(A) in FP64 (product of the pivots).
 constexpr int kRegNV = 2;
 // largest n of the register path: 5 under the 64-register bound of the FP32
-// kernels (more spills), 6 for FP64 (128 registers)
+// kernels (more spills); the FP64 kernel keeps the shared-memory LU (its
+// register file is full with the FP64 electron phase: the register path
+// measured 17 % slower there)
 template <typename R>
-constexpr int kRegMaxN = kMixed<R> ? 5 : 6;
+constexpr int kRegMaxN = kMixed<R> ? 5 : 0;
 
 template <typename R, int N>
 __device__ inline double lu_solve_regs(R* rows, int64_t rs, int64_t cs, int nv) {
@@ -569,6 +571,7 @@ template <typename R>
 __device__ inline bool lu_solve_regs_n(R* rows, int64_t rs, int64_t cs, int n, int nv,
                                        double* det) {
   if (nv > kRegNV || n > kRegMaxN<R>) return false;
+  if constexpr (kRegMaxN<R> < 1) return false;
   switch (n) {
     case 1: *det = lu_solve_regs<R, 1>(rows, rs, cs, nv); return true;
     case 2: *det = lu_solve_regs<R, 2>(rows, rs, cs, nv); return true;
@@ -577,14 +580,6 @@ __device__ inline bool lu_solve_regs_n(R* rows, int64_t rs, int64_t cs, int n, i
     case 5: *det = lu_solve_regs<R, 5>(rows, rs, cs, nv); return true;
     default: break;
   }
-  if constexpr (kRegMaxN<R> >= 6) {
-    switch (n) {
-      case 6: *det = lu_solve_regs<R, 6>(rows, rs, cs, nv); return true;
-
-
-      default: break;
-    }
-  }
   return false;
 }
 
@@ -592,19 +587,18 @@ __device__ inline bool lu_solve_regs_n(R* rows, int64_t rs, int64_t cs, int n, i
 // slater_pooling.py:147-260) from X = A^-1 A_virt: 1 (ground state), X_ij
 // (single), det of the 2 x 2 block of X (double).
 template <typename R, typename T>
-__device__ inline void excitation_values(const qmc_wf_desc& d, int spin, CView<R> X, int nv,
-                                         T* dv, int64_t s) {
+__device__ inline void excitation_values(const qmc_wf_desc& d, const int* tab, int spin,
+                                         CView<R> X, int nv, T* dv, int64_t s) {
   const int nd = d.ndet[spin];
-  const int* tab = d.det_table[spin];
   for (int u = 0; u < nd; ++u) {
-    const int ord = __ldg(tab + 5 * u);
+    const int ord = tab[5 * u];
     R v = (R)1;
     if (ord == 1) {
-      const int i0 = __ldg(tab + 5 * u + 1);
+      const int i0 = tab[5 * u + 1];
       v = X(i0 / nv, i0 % nv);
     } else if (ord >= 2) {
-      const int i0 = __ldg(tab + 5 * u + 1), i1 = __ldg(tab + 5 * u + 2);
-      const int i2 = __ldg(tab + 5 * u + 3), i3 = __ldg(tab + 5 * u + 4);
+      const int i0 = tab[5 * u + 1], i1 = tab[5 * u + 2];
+      const int i2 = tab[5 * u + 3], i3 = tab[5 * u + 4];
       const R t00 = X(i0 / nv, i0 % nv), t01 = X(i1 / nv, i1 % nv);
       const R t10 = X(i2 / nv, i2 % nv), t11 = X(i3 / nv, i3 % nv);
       v = t00 * t11 - t01 * t10;
@@ -616,7 +610,7 @@ __device__ inline void excitation_values(const qmc_wf_desc& d, int spin, CView<R
 template <typename R, bool OP>
 __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned char* scr,
                               int64_t ss, int64_t w, int spin, R* mo_s, const R* bk_s, int wl,
-                              int nwb, double* dref) {
+                              int nwb, double* dref, const int* dtab) {
   using T = typename std::conditional<OP, double, R>::type;
   const int row0 = spin ? d.nup : 0;
   const int64_t cs = nwb, rs = (int64_t)d.nmo_used * nwb;
@@ -641,7 +635,8 @@ __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned 
     double det;
     if (n > 0 && lu_solve_regs_n<R>(rows, rs, cs, n, nv, &det)) {
       dref[spin * nwb + wl] = det;
-      excitation_values<R, T>(d, spin, CView<R>{rows + n * cs, rs, cs}, nv > 0 ? nv : 1, dv, ss);
+      excitation_values<R, T>(d, dtab, spin, CView<R>{rows + n * cs, rs, cs}, nv > 0 ? nv : 1,
+                              dv, ss);
       return;
     }
     wk.LU = MView<R>{rows, rs, cs};
@@ -689,7 +684,8 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   if (tid < 2 * nwb) {
     const int spin = tid / nwb, wl = tid - spin * nwb;
     if (w0 + wl < nw)
-      ep_det<R, KIN>(d, L, dbase, dss, dsm ? wl : w0 + wl, spin, MO, BK, wl, nwb, DREF);
+      ep_det<R, KIN>(d, L, dbase, dss, dsm ? wl : w0 + wl, spin, MO, BK, wl, nwb, DREF,
+                     t.det_tab[spin]);
   }
   __syncthreads();
   if (tid < nwb && w0 + tid < nw) {
@@ -700,7 +696,8 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
     const int64_t slot = dsm ? wl : w;
     const T* dv = rptr<T>(dbase, L.dv, dss, slot);
     const double* ov = KIN ? rptr<double>(dbase, L.ov, dss, slot) : nullptr;
-    const double psid = ci_combine<T, KIN, T>(d, dv, ov, dss, DREF[wl], DREF[nwb + wl], &kin);
+    const double psid = ci_combine<T, KIN, T>(d, t.cfg_det[0], t.cfg_det[1], t.ci_w, dv, ov, dss,
+                                              DREF[wl], DREF[nwb + wl], &kin);
     double logj = 0.0, v = 0.0;
     for (int e = 0; e < ne; ++e) {
       logj += JR[e * nwb + wl];
