@@ -73,6 +73,10 @@ def parse():
                    help="all-elec-iter sweeps per timed C6H6 launch (mixed method)")
     p.add_argument("--mc-steps", type=int, default=100)
     p.add_argument("--cpu-seconds", type=float, default=12.0)
+    p.add_argument("--kernels", action="store_true",
+                   help="time every kernel of the path once per precision on the workload "
+                        "(psi, local energy, pooling, potentials, gradients, adjoints) and exit: "
+                        "the launch list of the per-kernel profiles")
     return p.parse_args()
 
 
@@ -788,6 +792,63 @@ def run_gb300(args):
         dist.destroy_process_group()
 
 
+def run_kernels(args):
+    """Each kernel of the path on the workload (H2O cc-pVDZ single_double(4,4),
+    ``--nwalkers`` seeded positions after 200 FP64 Metropolis steps), both
+    precisions: CUDA-event time per call (mean of 3 after one warm-up), one JSON
+    line. The launch list a per-kernel ncu capture selects from."""
+    import torch
+
+    from qmctorch_gb300.sampler import Metropolis
+    from qmctorch_gb300.scf import Molecule
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    torch.set_default_dtype(torch.float64)
+    device = torch.device("cuda", 0)
+    mol = Molecule(H2O, unit="angs", basis="cc-pvdz")
+    fc = np.random.default_rng(7).uniform(size=27)
+    nw = args.nwalkers
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=device)
+    out = {"workload": "h2o_ccpvdz_single_double44_%dw" % nw, "ms": {}}
+    x = None
+    for prec in ("mixed", "fp64"):
+        wf = SlaterJastrow(mol, configs=CONFIGS, cuda=True, precision=prec)
+        wf.fc.weight.data = torch.as_tensor(fc, device=device).reshape(1, -1)
+        if x is None:
+            x = torch.as_tensor(seeded_positions(mol, nw, seed=0), device=device)
+            s = Metropolis(nwalkers=nw, nstep=200, step_size=STEP_SIZE, nelec=mol.nelec,
+                           init=mol.domain("atomic"), cuda=True, seed=3)
+            s.advance(wf.pdf if prec == "fp64" else SlaterJastrow(
+                mol, configs=CONFIGS, cuda=True, precision="fp64").pdf, x)
+        g = torch.as_tensor(np.random.default_rng(1).normal(size=nw), device=device)
+
+        def psi_adj():
+            for p_ in wf.parameters():
+                p_.grad = None
+            (wf(x).reshape(-1) * g).sum().backward()
+
+        def el_adj():
+            for p_ in wf.parameters():
+                p_.grad = None
+            (wf.local_energy(x).reshape(-1) * g).sum().backward()
+
+        with torch.no_grad():
+            mo = wf.mo(wf.ao(x))
+        calls = {"psi": lambda: wf(x), "local_energy": lambda: wf.local_energy(x),
+                 "pooling": lambda: wf.pool(mo), "potentials": lambda: wf._potentials(x),
+                 "gradients": lambda: wf.gradients_jacobi(x), "psi_adjoint": psi_adj,
+                 "local_energy_adjoint": el_adj}
+        for name, fn in calls.items():
+            if prec == "mixed" and name in ("pooling", "potentials", "gradients",
+                                            "psi_adjoint", "local_energy_adjoint"):
+                continue  # FP64 kernels whatever the method
+            with torch.no_grad() if "adjoint" not in name else torch.enable_grad():
+                fn()
+                torch.cuda.synchronize()
+                t = _timed(torch, lambda i: fn(), 3, flush) / 3
+            out["ms"]["%s_%s" % (name, prec)] = t * 1e3
+    print(json.dumps(out))
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -815,5 +876,7 @@ if __name__ == "__main__":
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.kernels:
+        run_kernels(a)
     else:
         run_gb300(a)
