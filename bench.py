@@ -96,7 +96,9 @@ def _cpu_worker(args):
     _os.environ.setdefault("OMP_NUM_THREADS", "1")
     from oracle import qmc_oracle as orc
     from qmctorch_gb300.scf import Molecule
-    mol = Molecule(H2O, unit="angs", basis="cc-pvdz")
+    # the Hueckel orbitals: the oracle's arithmetic does not depend on the MO
+    # values, and the SCF of each worker would fall inside the timed wall
+    mol = Molecule(H2O, unit="angs", basis="cc-pvdz", calculator="huckel")
     rng = np.random.default_rng(seed)
     fc = np.random.default_rng(7).uniform(size=27)
     wf = orc.OracleSlaterJastrow(mol, configs=CONFIGS, fc_weight=fc)
@@ -745,7 +747,7 @@ def run_gb300(args):
             "scaling": "weak",
             "vs_baseline": None,
             "dtype": "f32+f64 (mixed)",
-            "data": "synthetic (seeded walker positions; built-in cc-pVDZ tables, extended-Hueckel MOs)",
+            "data": "synthetic (seeded walker positions; built-in cc-pVDZ tables, RHF MOs of this package's SCF)",
             "config": workload_config(args, nw),
             # compute roofline of the dominant kernel: counted flops per walker-step
             # (count_fp64_flops_per_psi: the work of one psi evaluation) x walker-steps

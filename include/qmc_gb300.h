@@ -387,6 +387,35 @@ int64_t qmc_reduce_scratch_bytes(int64_t n);
 int qmc_reduce_stats(const double* x, int64_t n, double* stats, void* scratch,
                      int64_t scratch_bytes, void* stream);
 
+/*
+ * Restricted Hartree-Fock integrals (host code, host pointers). The reference
+ * takes its molecular orbitals from pyscf (RHF, qmctorch/scf/calculator/
+ * pyscf.py:88-103); these replace pyscf's integrals over the basis functions
+ * exactly as the AO layer evaluates them:
+ *   chi_mu(r) = sum_{p : prim_ao[p] = mu} prim_coef[p] x^kx y^ky z^kz exp(-prim_exp[p] |r - C_p|^2)
+ * (x, y, z relative to the centre C_p, cartesian powers prim_k[p*3..], total
+ * degree <= 2). McMurchie-Davidson recursions, Boys function from its series.
+ */
+typedef struct qmc_gto_basis {
+  int32_t nao;               /* contracted functions */
+  int32_t nprim;             /* primitive entries */
+  const int32_t* prim_ao;    /* [nprim] function of each entry */
+  const double* prim_center; /* [nprim*3] */
+  const double* prim_exp;    /* [nprim] */
+  const double* prim_coef;   /* [nprim] contraction coefficient x primitive norm */
+  const int32_t* prim_k;     /* [nprim*3] cartesian powers */
+} qmc_gto_basis;
+
+/* Overlap S, kinetic energy T and nuclear attraction V (-sum_C Z_C / |r - C|),
+   each [nao*nao], of the basis over natom point charges. */
+int qmc_scf_one_electron(const qmc_gto_basis* b, int32_t natom, const double* atom_xyz,
+                         const double* atom_z, double* S, double* T, double* V);
+
+/* Electron repulsion integrals (mu nu | la si) = eri[((mu*n + nu)*n + la)*n + si]
+   (chemists' notation, all nao^4 entries, 8-fold symmetry filled; quartets whose
+   Schwarz bound is below 1e-14 are 0). Threads: all host cores. */
+int qmc_scf_eri(const qmc_gto_basis* b, double* eri);
+
 /* Human-readable status. */
 const char* qmc_status_string(int status);
 

@@ -23,7 +23,8 @@ BUILD = os.path.join(ROOT, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
-           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu", "qmc_reduce.cu", "qmc_mo_tc.cu"]
+           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu", "qmc_reduce.cu", "qmc_mo_tc.cu",
+           "qmc_scf.cpp"]
 # translation units compiled more than once, with defines: (source, object, flags)
 INSTANCES = [("qmc_metropolis_inst.cu", "qmc_metropolis_%s_%d" % (r, jc),
               ["-DQMC_INST_R=%s" % r, "-DQMC_INST_JC=%d" % jc])
@@ -64,7 +65,7 @@ def build(force=False, verbose=False):
             print(r.stdout + r.stderr)
         return obj
 
-    units = [(src, src[:-3], []) for src in SOURCES] + INSTANCES
+    units = [(src, os.path.splitext(src)[0], []) for src in SOURCES] + INSTANCES
     # longest first: the Metropolis and sweep units set the wall time
     units.sort(key=lambda u: ("inst" not in u[0], "sweep" not in u[0]))
     with ThreadPoolExecutor(max_workers=min(len(units), os.cpu_count() or 4)) as ex:
@@ -106,6 +107,12 @@ class WfDesc(ctypes.Structure):
     ]
 
 
+class GtoBasis(ctypes.Structure):
+    _fields_ = [("nao", c_int32), ("nprim", c_int32), ("prim_ao", c_void_p),
+                ("prim_center", c_void_p), ("prim_exp", c_void_p), ("prim_coef", c_void_p),
+                ("prim_k", c_void_p)]
+
+
 class MetropolisArgs(ctypes.Structure):
     _fields_ = [
         ("pos", c_void_p), ("nwalkers", c_int64), ("nstep", c_int32), ("ntherm", c_int32),
@@ -134,6 +141,9 @@ SIGNATURES = {
     "qmc_mo_eval": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_mo_eval_tc": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_mo_eval_tc_status": (ctypes.c_int, [c_void_p]),
+    "qmc_scf_one_electron": (ctypes.c_int, [_P(GtoBasis), c_int32, c_void_p, c_void_p, c_void_p,
+                                            c_void_p, c_void_p]),
+    "qmc_scf_eri": (ctypes.c_int, [_P(GtoBasis), c_void_p]),
     "qmc_jastrow_en": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p,
                                       c_void_p, c_int32, c_void_p]),
     "qmc_set_wait_limit_ns": (ctypes.c_uint64, [ctypes.c_uint64]),

@@ -16,11 +16,14 @@ the same entry layout:
   entry, ``nao_per_atom``, ``nctr_per_ao`` (``pyscf.py:206-223``);
 * ``mos`` column-normalised (``calculator_base.py:36-46``).
 
-Molecular orbitals come from an extended-Hueckel guess (Wolfsberg-Helmholz,
-K = 1.75) on the overlap matrix of the AOs exactly as the AO layer evaluates
-them; there is no Hartree-Fock solver here. ``nmo`` keeps the reference's
-count of spherical MOs (a d shell contributes 5), so the lowest ``nmo``
-Hueckel orbitals are kept.
+Molecular orbitals: ``calculator="pyscf"`` (the reference's default) runs
+this package's restricted Hartree-Fock (``rhf.py``: native McMurchie-Davidson
+integrals over the AOs as the AO layer evaluates them, SCF in the span of the
+real solid harmonics like pyscf's spherical basis); ``calculator="huckel"``
+(or ``"builtin"``) keeps the extended-Hueckel guess (Wolfsberg-Helmholz,
+K = 1.75) on the overlap matrix, which is also the SCF's starting density.
+``nmo`` is the reference's count of spherical MOs (a d shell contributes 5).
+SCF results are cached per (atoms, coordinates, basis) for the process.
 """
 from __future__ import annotations
 
@@ -213,14 +216,35 @@ def huckel_mos(basis, atoms, atom_coords, k_wh=1.75):
     return mos, evals[: basis.nmo]
 
 
+_SCF_CACHE = {}
+
+
+def scf_orbitals(basis, atoms, atom_coords, charges, nelec):
+    """RHF orbitals of the namespace (cached): (mos, mo_energy, total energy)."""
+    from .rhf import rhf
+    key = (tuple(atoms), tuple(np.round(np.asarray(atom_coords, dtype=np.float64), 12).ravel()),
+           basis.nao, basis.nmo, tuple(np.round(basis.bas_exp, 12)), nelec)
+    if key not in _SCF_CACHE:
+        guess, _ = huckel_mos(basis, atoms, atom_coords)
+        mos, mo_energy, etot, converged = rhf(basis, atom_coords, charges, nelec, guess=guess)
+        if not converged:
+            raise RuntimeError("RHF did not converge for %s" % "".join(atoms))
+        if len(_SCF_CACHE) > 256:
+            _SCF_CACHE.clear()
+        _SCF_CACHE[key] = (mos, mo_energy, etot)
+    mos, mo_energy, etot = _SCF_CACHE[key]
+    return mos.copy(), mo_energy.copy(), etot
+
+
 class Molecule:
     """Drop-in for ``qmctorch.scf.Molecule`` (``qmctorch/scf/molecule.py:22-162``)
     restricted to what the hot path reads: ``nelec, nup, ndown, spin, natom,
     atoms, atomic_number, atomic_nelec, atom_coords, hdf5file, basis``.
 
-    ``calculator`` may be ``"pyscf"`` or ``"builtin"``; both use the built-in
-    tables and the Hueckel MO guess (pyscf is not installed). ``load`` accepts a
-    ``.npz`` file written by :meth:`save`.
+    ``calculator``: ``"pyscf"`` (default, RHF orbitals as the reference's pyscf
+    calculator provides them, computed by this package) or ``"huckel"`` /
+    ``"builtin"`` (extended-Hueckel guess); both on the built-in basis tables.
+    ``load`` accepts a ``.npz`` file written by :meth:`save`.
     """
 
     def __init__(self, atom=None, calculator="pyscf", scf="hf", basis="sto-3g",
@@ -243,8 +267,8 @@ class Molecule:
             return
         if unit not in ("angs", "bohr"):
             raise ValueError("unit should be angs or bohr")
-        if calculator not in ("pyscf", "builtin"):
-            raise ValueError("only the built-in GTO tables are available (calculator='pyscf')")
+        if calculator not in ("pyscf", "builtin", "huckel"):
+            raise ValueError("calculator must be 'pyscf' (RHF) or 'huckel'")
         for a in atom.split(";"):
             if not a.strip():
                 continue
@@ -269,8 +293,12 @@ class Molecule:
             self.name = "".join(self.atoms)
         self.hdf5file = "_".join([self.name, calculator, basis]) + ".hdf5"
         self.basis = build_basis_namespace(self.atoms, self.atom_coords, basis)
-        self.basis.mos, self.basis.mo_energy = huckel_mos(self.basis, self.atoms,
-                                                          self.atom_coords)
+        if calculator == "pyscf" and self.spin == 0:
+            self.basis.mos, self.basis.mo_energy, self.basis.TotalEnergy = scf_orbitals(
+                self.basis, self.atoms, self.atom_coords, self.atomic_number, self.nelec)
+        else:
+            self.basis.mos, self.basis.mo_energy = huckel_mos(self.basis, self.atoms,
+                                                              self.atom_coords)
         self.atoms = np.array(self.atoms)
 
     def domain(self, method):
