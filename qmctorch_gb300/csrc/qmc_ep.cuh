@@ -32,6 +32,19 @@ struct EPLayout {
   int nmax, vmax, omax;
 };
 
+// The mixed local energy solves a spin channel in registers (el_channel_regs)
+// for excitation expansions with at most 5 electrons and 2 virtual orbitals
+// per spin (H2O cc-pVDZ with single_double(4,4): 5 and 2).
+constexpr int kElRegMaxN = 5, kElRegNV = 2;
+__host__ __device__ inline bool el_regs(const qmc_wf_desc& d) {
+  if (d.precision != QMC_PREC_MIXED || d.det_mode != QMC_DET_EXCITATION) return false;
+  for (int s = 0; s < 2; ++s) {
+    const int n = s ? d.ndown : d.nup;
+    if (n < 1 || n > kElRegMaxN || d.max_orb[s] - n > kElRegNV || d.max_orb[s] < n) return false;
+  }
+  return true;
+}
+
 __host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
   EPLayout L;
   const bool mixed = d.precision == QMC_PREC_MIXED;
@@ -55,15 +68,18 @@ __host__ __device__ inline EPLayout ep_layout(const qmc_wf_desc& d, int kind) {
   };
   const bool el = kind == 1;
   // psi / Metropolis in excitation mode factor the Slater matrix in place in
-  // the block's shared-memory MO rows (ep_det): no LU or A^-1 A_virt arrays
-  const bool inplace = !el && d.det_mode == QMC_DET_EXCITATION;
+  // the block's shared-memory MO rows (ep_det): no LU or A^-1 A_virt arrays;
+  // the mixed local energy of small excitation expansions solves in
+  // registers (el_channel_regs): only the determinant and trace values
+  const bool inplace = (!el && d.det_mode == QMC_DET_EXCITATION) || (el && el_regs(d));
+  const bool work = !inplace || !el;  // the E_L work arrays, unless in registers
   for (int s = 0; s < 2; ++s) {
     add(L.lu[s], inplace ? 0 : (int64_t)nmax * nmax, rsz);
     add(L.x[s], inplace ? 0 : (int64_t)nmax * vmax, rsz);
-    add(L.y[s], el ? (int64_t)nmax * omax : 0, rsz);
-    add(L.x64[s], (el && mixed) ? (int64_t)nmax * vmax : 0, 8);
-    add(L.y64[s], (el && mixed) ? (int64_t)nmax * omax : 0, 8);
-    add(L.rc[s], (el && mixed) ? nmax : 0, rsz);
+    add(L.y[s], (el && work) ? (int64_t)nmax * omax : 0, rsz);
+    add(L.x64[s], (el && mixed && work) ? (int64_t)nmax * vmax : 0, 8);
+    add(L.y64[s], (el && mixed && work) ? (int64_t)nmax * omax : 0, 8);
+    add(L.rc[s], (el && mixed && work) ? nmax : 0, rsz);
   }
   add(L.dv, d.ndet[0] + d.ndet[1], el ? 8 : rsz);
   add(L.ov, el ? d.ndet[0] + d.ndet[1] : 0, 8);
@@ -607,6 +623,206 @@ __device__ inline void excitation_values(const qmc_wf_desc& d, const int* tab, i
   }
 }
 
+// Row interchanges of a solve: the pivots of the factorisation applied to x
+// in order (lu_solve's pivot pass), with selects on the register array.
+template <typename R, int N>
+__device__ __forceinline__ void apply_pivots(const int (&piv)[N], R (&x)[N]) {
+#pragma unroll
+  for (int k = 0; k < N; ++k)
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const bool sw = piv[k] == i;
+      const R a = x[k], b = x[i];
+      x[k] = sw ? b : a;
+      x[i] = sw ? a : b;
+    }
+}
+
+// Forward and back substitution with the factors a[0..N)[0..N) (unit lower,
+// upper with inverted diagonal), lu_solve's order.
+template <typename R, int N, int NC>
+__device__ __forceinline__ void lu_subst(const R (&a)[N][NC], R (&x)[N]) {
+#pragma unroll
+  for (int i = 1; i < N; ++i) {
+    R s = x[i];
+#pragma unroll
+    for (int k = 0; k < i; ++k) s = fma(-a[i][k], x[k], s);
+    x[i] = s;
+  }
+#pragma unroll
+  for (int i = N - 1; i >= 0; --i) {
+    R s = x[i];
+#pragma unroll
+    for (int k = i + 1; k < N; ++k) s = fma(-a[i][k], x[k], s);
+    x[i] = s * a[i][i];
+  }
+}
+
+// Local-energy determinant phase of one (walker, spin) channel, mixed method,
+// excitation mode (spin_channel with OP and the refinement, slater_pooling.py:
+// 147-260, 437-723), with the LU, the solves and their FP64 refinement in
+// registers: the operations of spin_channel in the same order (bitwise the
+// same values) without its HBM work arrays. mo / bk: the spin's MO and
+// kinetic rows in shared memory. Writes the determinant values (relative to
+// det A, FP64) and traces per unique determinant, and det A to *dref.
+template <typename R, int N>
+__device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> mo, CView<R> bk,
+                                       int nv, const int* tab, double* dv, double* ov, int64_t s,
+                                       double* dref) {
+  constexpr int NC = N + kElRegNV;
+  R a[N][NC];
+#pragma unroll
+  for (int i = 0; i < N; ++i)
+#pragma unroll
+    for (int j = 0; j < NC; ++j) a[i][j] = (j < N + nv) ? mo(i, j) : (R)0;
+  int piv[N];
+  double det = 1.0;
+#pragma unroll
+  for (int k = 0; k < N; ++k) {
+    int p = k;
+    R amax = fabs(a[k][k]);
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const R v = fabs(a[i][k]);
+      if (v > amax) {
+        amax = v;
+        p = i;
+      }
+    }
+    piv[k] = p;
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const bool sw = (i == p);
+#pragma unroll
+      for (int j = 0; j < NC; ++j) {
+        const R x = a[k][j], y = a[i][j];
+        a[k][j] = sw ? y : x;
+        a[i][j] = sw ? x : y;
+      }
+    }
+    if (p != k) det = -det;
+    const R akk = a[k][k];
+    det *= (double)akk;
+    const R inv = akk != (R)0 ? (R)1 / akk : (R)0;
+    a[k][k] = inv;
+#pragma unroll
+    for (int i = k + 1; i < N; ++i) {
+      const R l = a[i][k] * inv;
+      a[i][k] = l;
+#pragma unroll
+      for (int j = k + 1; j < N; ++j) a[i][j] = fma(-l, a[k][j], a[i][j]);
+    }
+  }
+  *dref = det;
+  // residual of a solve x of column b (b in the original row order), corrected
+  // with the FP32 factors, in FP64 (lu_refine)
+  auto refine = [&](const R (&b)[N], const R (&x)[N], double (&x64)[N]) {
+    R rc[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      double r = (double)b[i];
+#pragma unroll
+      for (int k = 0; k < N; ++k) r = fma(-(double)mo(i, k), (double)x[k], r);
+      rc[i] = (R)r;
+    }
+    apply_pivots<R, N>(piv, rc);
+    lu_subst<R, N, NC>(a, rc);
+#pragma unroll
+    for (int i = 0; i < N; ++i) x64[i] = (double)x[i] + (double)rc[i];
+  };
+  // X = A^-1 A_virt (the virtual columns were interchanged with the rows)
+  double x64[N][kElRegNV];
+#pragma unroll
+  for (int c = 0; c < kElRegNV; ++c) {
+    if (c >= nv) break;
+    R x[N], b[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      x[i] = a[i][N + c];
+      b[i] = mo(i, N + c);
+    }
+    lu_subst<R, N, NC>(a, x);
+    double y[N];
+    refine(b, x, y);
+#pragma unroll
+    for (int i = 0; i < N; ++i) x64[i][c] = y[i];
+  }
+  // Y = A^-1 [B_occ | B_virt], refined: trace of the occupied block and
+  // M = Y_virt - Y_occ X (virtual columns first, then the occupied columns
+  // subtracted in order, as M is formed element by element)
+  double m64[N][kElRegNV];
+  double base = 0.0;
+#pragma unroll
+  for (int cc = 0; cc < N + kElRegNV; ++cc) {
+    const int c = cc < kElRegNV ? N + cc : cc - kElRegNV;  // virtual, then occupied
+    if (cc < kElRegNV && cc >= nv) continue;
+    R b[N], x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) b[i] = x[i] = bk(i, c);
+    apply_pivots<R, N>(piv, x);
+    lu_subst<R, N, NC>(a, x);
+    double y[N];
+    refine(b, x, y);
+    if (cc < kElRegNV) {
+#pragma unroll
+      for (int i = 0; i < N; ++i) m64[i][cc] = y[i];
+    } else {
+      base += y[c];
+#pragma unroll
+      for (int ic = 0; ic < kElRegNV; ++ic) {
+        if (ic >= nv) break;
+#pragma unroll
+        for (int i = 0; i < N; ++i) m64[i][ic] = fma(-y[i], x64[c][ic], m64[i][ic]);
+      }
+    }
+  }
+  // excitation determinants and traces (spin_channel's loop with OP); entries
+  // of order >= 1 exist only when there are virtual columns
+  const int nd = d.ndet[spin];
+  nv = nv > 0 ? nv : 1;
+  for (int u = 0; u < nd; ++u) {
+    const int ord = tab[5 * u];
+    double dvu = 1.0, ovu = base;
+    if (ord == 1) {
+      const int i0 = tab[5 * u + 1];
+      const double m = x64[i0 / nv][i0 % nv];
+      dvu = m;
+      ovu = fma(1.0 / m, m64[i0 / nv][i0 % nv], base);
+    } else if (ord >= 2) {
+      const int i0 = tab[5 * u + 1], i1 = tab[5 * u + 2];
+      const int i2 = tab[5 * u + 3], i3 = tab[5 * u + 4];
+      const double t00 = x64[i0 / nv][i0 % nv], t01 = x64[i1 / nv][i1 % nv];
+      const double t10 = x64[i2 / nv][i2 % nv], t11 = x64[i3 / nv][i3 % nv];
+      const double dt = t00 * t11 - t01 * t10;
+      dvu = dt;
+      const double m00 = m64[i0 / nv][i0 % nv], m01 = m64[i1 / nv][i1 % nv];
+      const double m10 = m64[i2 / nv][i2 % nv], m11 = m64[i3 / nv][i3 % nv];
+      const double idt = 1.0 / dt;
+      ovu = base + idt * (t11 * m00 - t01 * m10 - t10 * m01 + t00 * m11);
+    }
+    dv[u * s] = dvu;
+    ov[u * s] = ovu;
+  }
+}
+
+template <typename R>
+__device__ inline bool el_channel_regs_n(const qmc_wf_desc& d, int spin, CView<R> mo,
+                                         CView<R> bk, int n, int nv, const int* tab, double* dv,
+                                         double* ov, int64_t s, double* dref) {
+  if constexpr (!kMixed<R>) {
+    return false;
+  } else {
+    switch (n) {
+      case 1: el_channel_regs<R, 1>(d, spin, mo, bk, nv, tab, dv, ov, s, dref); return true;
+      case 2: el_channel_regs<R, 2>(d, spin, mo, bk, nv, tab, dv, ov, s, dref); return true;
+      case 3: el_channel_regs<R, 3>(d, spin, mo, bk, nv, tab, dv, ov, s, dref); return true;
+      case 4: el_channel_regs<R, 4>(d, spin, mo, bk, nv, tab, dv, ov, s, dref); return true;
+      case 5: el_channel_regs<R, 5>(d, spin, mo, bk, nv, tab, dv, ov, s, dref); return true;
+      default: return false;
+    }
+  }
+}
+
 template <typename R, bool OP>
 __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned char* scr,
                               int64_t ss, int64_t w, int spin, R* mo_s, const R* bk_s, int wl,
@@ -625,6 +841,16 @@ __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned 
   wk.X64 = MView<double>{rptr<double>(scr, L.x64[spin], ss, w), vm * ss, ss};
   wk.Y64 = MView<double>{rptr<double>(scr, L.y64[spin], ss, w), (int64_t)L.omax * ss, ss};
   T* dv = rptr<T>(scr, L.dv, ss, w) + (spin ? d.ndet[0] * ss : 0);
+  if constexpr (OP) {
+    if (el_regs(d)) {
+      const int n = spin ? d.ndown : d.nup;
+      double* ovp = rptr<double>(scr, L.ov, ss, w) + (spin ? d.ndet[0] * ss : 0);
+      const int nv = d.max_orb[spin] - n;
+      if (el_channel_regs_n<R>(d, spin, mo, bk, n, nv, dtab, (double*)dv, ovp, ss,
+                               &dref[spin * nwb + wl]))
+        return;
+    }
+  }
   if (!OP && d.det_mode == QMC_DET_EXCITATION) {
     // in place (the MO rows are recomputed before every evaluation): the LU of
     // the occupied columns and A^-1 A_virt over the virtual columns of the
