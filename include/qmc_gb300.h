@@ -122,7 +122,19 @@ typedef struct qmc_wf_desc {
   int32_t use_jastrow_en;
   const double* jastrow_en_w;     /* [1] (jastrow_kernel.weight of the e-n factor) */
   const double* jastrow_en_atoms; /* [natom*3] nucleus positions of the e-n factor */
+  /* Radial part of the AOs (AtomicOrbitals.radial, radial_functions.py):
+     QMC_RADIAL_GTO sums exp(-a r^2) (radial_gaussian_pure 241-320, the pyscf
+     layout), QMC_RADIAL_STO is r^kr exp(-a r) (radial_slater 6-123, the ADF
+     layout with cartesian harmonics), QMC_RADIAL_STO_PURE is exp(-a r)
+     (radial_slater_pure 323-406). ao_kr: [nao] power of r of each AO (STO),
+     may be NULL for GTO. */
+  int32_t radial_type;
+  const int32_t* ao_kr;
 } qmc_wf_desc;
+
+#define QMC_RADIAL_GTO 0
+#define QMC_RADIAL_STO 1
+#define QMC_RADIAL_STO_PURE 2
 
 /* Scratch bytes for nwalkers walkers; kind 0 = psi, 1 = local energy. */
 int64_t qmc_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers, int32_t kind);

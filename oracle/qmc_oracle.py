@@ -37,6 +37,9 @@ class OracleBasis:
         self.bas_exp = np.asarray(basis.bas_exp if bas_exp is None else bas_exp, dtype=np.float64)
         self.k = np.stack([np.asarray(basis.bas_kx), np.asarray(basis.bas_ky),
                            np.asarray(basis.bas_kz)], axis=1).astype(np.int64)
+        self.radial = str(getattr(basis, "radial_type", "gto_pure"))
+        self.kr = np.asarray(getattr(basis, "bas_kr", np.zeros(len(self.bas_exp))),
+                             dtype=np.float64)
         # norm_orbital.py:136-161, computed from the namespace exponents once
         # (atomic_orbitals.py:93-94)
         a = np.asarray(basis.bas_exp, dtype=np.float64)
@@ -46,6 +49,16 @@ class OracleBasis:
             df = np.array([DF[int(2 * v - 1)] for v in kd], dtype=np.float64)
             norm = norm * (4.0 * a) ** (kd / 2.0) / np.sqrt(df)
         self.norm_cst = norm
+        if self.radial.startswith("sto"):
+            # norm_slater_cartesian (norm_orbital.py:106-161)
+            kk = self.k
+            lv = kk.sum(1) + self.kr + 1.0
+            lfact = np.array([float(np.prod(np.arange(1, int(2 * v) + 1))) for v in lv])
+            pref = 4.0 * np.pi * lfact / (2.0 * a) ** (2.0 * lv + 1.0)
+            num = np.prod(np.array([[DF[int(2 * v - 1)] for v in row] for row in kk],
+                                   dtype=np.float64), axis=1)
+            den = np.array([DF[int(2 * s_ + 1)] for s_ in kk.sum(1)], dtype=np.float64)
+            self.norm_cst = np.sqrt(1.0 / (pref * num / den))
         # index_add of the contraction (atomic_orbitals.py:654-669) as a
         # (primitive x AO) matrix of the bas_coeffs
         self.contraction = np.zeros((len(self.index_ctr), self.nao))
@@ -82,6 +95,8 @@ def ao_values(b: OracleBasis, pos, derivative=0, sum_grad=True):
     xyz = np.repeat(xyz, b.nshells, axis=2)
     r = np.repeat(r, b.nshells, axis=2)
     alpha = b.bas_exp
+    if b.radial.startswith("sto"):
+        return _sto_ao_values(b, xyz, r, derivative, sum_grad, nb, ne)
     # radial_gaussian_pure
     R2 = r * r
     er = np.exp(-alpha * R2)
@@ -142,6 +157,51 @@ def ao_values(b: OracleBasis, pos, derivative=0, sum_grad=True):
         return lap_kernel(nabla_er, lap_er, dY, d2Y)
     if list(derivative) == [0, 1, 2]:
         return ao_kernel(), grad_kernel(nabla_er, dY), lap_kernel(nabla_er, lap_er, dY, d2Y)
+    raise ValueError("derivative must be 0, 1, 2 or [0, 1, 2]")
+
+
+def _sto_ao_values(b, xyz, r, derivative, sum_grad, nb, ne):
+    """Slater-type AOs (radial_slater / radial_slater_pure,
+    radial_functions.py:6-123, 323-406) times cartesian harmonics, combined
+    as atomic_orbitals.py:236-423 combines radial and angular parts; the ADF
+    layout is uncontracted (one entry per AO, coefficients 1)."""
+    alpha = b.bas_exp
+    n = b.kr if b.radial == "sto" else np.zeros_like(b.kr)
+    k = b.k
+    er = np.exp(-alpha * r)
+    rn = r ** n
+    R = rn * er
+    xyz_k = _fast_power(xyz, k)
+    Y = xyz_k.prod(-1)
+    nc = b.norm_cst
+    if derivative == 0 or derivative == [0]:
+        return nc * R * Y
+    nrm2 = n * r ** (n - 2)
+    nabla_rn = nrm2[..., None] * xyz
+    nabla_er = -(alpha * er)[..., None] * xyz / r[..., None]
+    nabla_R = nabla_rn * er[..., None] + rn[..., None] * nabla_er
+    lap_R = (nrm2 * (n + 1)) * er + 2.0 * (nabla_rn * nabla_er).sum(-1) \
+        + rn * (alpha * er) * (alpha - 2.0 / r)
+    km1 = np.maximum(k - 1, 0)
+    km2 = np.maximum(k - 2, 0)
+    xyz_km1 = _fast_power(xyz, km1)
+    xyz_km2 = _fast_power(xyz, km2)
+    kx, ky, kz = k[:, 0], k[:, 1], k[:, 2]
+    dY = np.stack((kx * xyz_km1[..., 0] * xyz_k[..., 1] * xyz_k[..., 2],
+                   ky * xyz_k[..., 0] * xyz_km1[..., 1] * xyz_k[..., 2],
+                   kz * xyz_k[..., 0] * xyz_k[..., 1] * xyz_km1[..., 2]), axis=-1)
+    d2Y = (kx * (kx - 1) * xyz_km2[..., 0] * xyz_k[..., 1] * xyz_k[..., 2]
+           + ky * (ky - 1) * xyz_k[..., 0] * xyz_km2[..., 1] * xyz_k[..., 2]
+           + kz * (kz - 1) * xyz_k[..., 0] * xyz_k[..., 1] * xyz_km2[..., 2])
+    val = nc * R * Y
+    grad = nc[:, None] * (nabla_R * Y[..., None] + R[..., None] * dY)
+    lap = nc * (lap_R * Y + 2.0 * (nabla_R * dY).sum(-1) + R * d2Y)
+    if derivative == 1 or derivative == [1]:
+        return grad.sum(-1) if sum_grad else grad
+    if derivative == 2 or derivative == [2]:
+        return lap
+    if list(derivative) == [0, 1, 2]:
+        return val, grad, lap
     raise ValueError("derivative must be 0, 1, 2 or [0, 1, 2]")
 
 

@@ -104,6 +104,7 @@ class WfDesc(ctypes.Structure):
         ("ndet", c_int32 * 2), ("det_table", c_void_p * 2), ("cfg_det", c_void_p * 2),
         ("ci_weight", c_void_p), ("e_nuc", ctypes.c_double),
         ("use_jastrow_en", c_int32), ("jastrow_en_w", c_void_p), ("jastrow_en_atoms", c_void_p),
+        ("radial_type", c_int32), ("ao_kr", c_void_p),
     ]
 
 

@@ -207,7 +207,13 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
           const double vs = t.vscale ? t.vscale[a] : 1.0;
           for (int p = 0; p < np; ++p) {
             const int wi = t.ao_wofs[a] + p;
-            const double dao = -vs * t.wd[wi] * pl.p * r2 * exp(-t.walpha[wi] * r2);
+            double dao;
+            if (t.radial != QMC_RADIAL_GTO)  // Slater type: d/d alpha r^n e^(-alpha r)
+              dao = vs * t.wd[wi] *
+                    sto_dalpha(pl.p, 0.0, 0.0, 0.0, 0.0, 0, dx, dy, dz, r2, t.ao_kr[a],
+                               t.walpha[wi]).v;
+            else
+              dao = -vs * t.wd[wi] * pl.p * r2 * exp(-t.walpha[wi] * r2);
             accE[(int64_t)__ldg(w_entry + wi) * ss] += gw * h * dao;
           }
         }
@@ -533,15 +539,27 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
           const double vs = t.vscale ? t.vscale[a] : 1.0;
           for (int p = 0; p < np; ++p) {
             const int wi = t.ao_wofs[a] + p;
-            const double al = t.walpha[wi], wp = t.wd[wi], ep = exp(-al * r2);
-            const double q = 1.0 - al * r2;
-            const double dval = -vs * wp * pl.p * r2 * ep;
-            const double dgx = wp * ep * (-r2 * pl.dx - 2.0 * dx * pl.p * q);
-            const double dgy = wp * ep * (-r2 * pl.dy - 2.0 * dy * pl.p * q);
-            const double dgz = wp * ep * (-r2 * pl.dz - 2.0 * dz * pl.p * q);
-            const double dlap = vs * wp * ep *
-                                (-r2 * pl.lap + pl.p * (8.0 * r2 * al - 4.0 * r2 * r2 * al * al -
-                                                        (double)(6 + 4 * l) * q));
+            const double al = t.walpha[wi], wp = t.wd[wi];
+            double dval, dgx, dgy, dgz, dlap;
+            if (t.radial != QMC_RADIAL_GTO) {  // Slater type
+              const StoDAlpha sd = sto_dalpha(pl.p, pl.dx, pl.dy, pl.dz, pl.lap, l, dx, dy, dz,
+                                              r2, t.ao_kr[a], al);
+              dval = vs * wp * sd.v;
+              dgx = wp * sd.gx;
+              dgy = wp * sd.gy;
+              dgz = wp * sd.gz;
+              dlap = vs * wp * sd.lap;
+            } else {
+              const double ep = exp(-al * r2);
+              const double q = 1.0 - al * r2;
+              dval = -vs * wp * pl.p * r2 * ep;
+              dgx = wp * ep * (-r2 * pl.dx - 2.0 * dx * pl.p * q);
+              dgy = wp * ep * (-r2 * pl.dy - 2.0 * dy * pl.p * q);
+              dgz = wp * ep * (-r2 * pl.dz - 2.0 * dz * pl.p * q);
+              dlap = vs * wp * ep *
+                     (-r2 * pl.lap + pl.p * (8.0 * r2 * al - 4.0 * r2 * r2 * al * al -
+                                             (double)(6 + 4 * l) * q));
+            }
             const double c = ha * dval - hb * (0.5 * dlap + gx * dgx + gy * dgy + gz * dgz);
             accE[(int64_t)__ldg(w_entry + wi) * ss] += c;
           }

@@ -348,6 +348,40 @@ __device__ __forceinline__ void ao_group(const Tables<R>& t, int g, R dx, R dy, 
   }
 }
 
+// The Slater-type AOs of group g (each AO sums its own primitives).
+template <typename R, bool DERIV, typename F>
+__device__ __forceinline__ void group_sto(const Tables<R>& t, int g, R dx, R dy, R dz, R r2,
+                                          F& f) {
+  const int np = t.group_prim[g + 1] - t.group_prim[g];
+  for (int a = t.group_ao[g]; a < t.group_ao[g + 1]; ++a) {
+    const int kx = t.ao_k[3 * a], ky = t.ao_k[3 * a + 1], kz = t.ao_k[3 * a + 2];
+    const R px = pk0(dx, kx), py = pk0(dy, ky), pz = pk0(dz, kz);
+    R qx = 0, qy = 0, qz = 0, lapP = 0;
+    if (DERIV) {
+      qx = pk1(dx, kx) * py * pz;
+      qy = px * pk1(dy, ky) * pz;
+      qz = px * py * pk1(dz, kz);
+      lapP = pk2(dx, kx) * py * pz + px * pk2(dy, ky) * pz + px * py * pk2(dz, kz);
+    }
+    const R vs = t.vscale ? t.vscale[a] : (R)1;
+    AOVal<R> o{};
+    for (int p = 0; p < np; ++p) {
+      const int wi = t.ao_wofs[a] + p;
+      const R wg = t.wd[wi];
+      const AOVal<R> q = sto_from<R, DERIV>(px * py * pz, qx, qy, qz, lapP, kx + ky + kz, dx, dy,
+                                            dz, r2, t.ao_kr[a], t.walpha[wi], vs * wg, wg);
+      o.v += q.v;
+      if (DERIV) {
+        o.gx += q.gx;
+        o.gy += q.gy;
+        o.gz += q.gz;
+        o.lap += q.lap;
+      }
+    }
+    f(a, o);
+  }
+}
+
 // All AOs of one electron (split coordinates ex, ey, ez); the electron-atom
 // difference is formed once per atom (groups are stored atom by atom).
 template <typename R, bool DERIV, typename F>
@@ -355,6 +389,7 @@ __device__ __forceinline__ void for_each_ao_ep(const Tables<R>& t, XP<R> ex, XP<
                                                F& f) {
   int last = -1;
   R dx = 0, dy = 0, dz = 0, r2 = 0;
+  const bool sto = t.radial != QMC_RADIAL_GTO;
   for (int g = 0; g < t.ngroup; ++g) {
     const int A = t.group_atom[g];
     if (A != last) {
@@ -364,7 +399,10 @@ __device__ __forceinline__ void for_each_ao_ep(const Tables<R>& t, XP<R> ex, XP<
       r2 = dx * dx + dy * dy + dz * dz;
       last = A;
     }
-    ao_group<R, DERIV>(t, g, dx, dy, dz, r2, f);
+    if (sto)
+      group_sto<R, DERIV>(t, g, dx, dy, dz, r2, f);
+    else
+      ao_group<R, DERIV>(t, g, dx, dy, dz, r2, f);
   }
 }
 

@@ -31,6 +31,8 @@ static inline int check_desc(const qmc_wf_desc* d) {
   if (!d->contract && !d->ao_wv) return QMC_ERR_ARG;
   if (d->use_jastrow && !d->jastrow_w) return QMC_ERR_ARG;
   if (d->use_jastrow_en && (!d->jastrow_en_w || !d->jastrow_en_atoms)) return QMC_ERR_ARG;
+  if (d->radial_type < QMC_RADIAL_GTO || d->radial_type > QMC_RADIAL_STO_PURE) return QMC_ERR_ARG;
+  if (d->radial_type == QMC_RADIAL_STO && !d->ao_kr) return QMC_ERR_ARG;
   if (d->nmo_used > d->nmo || d->nmo_used < 1) return QMC_ERR_ARG;
   if (d->det_mode != QMC_DET_EXCITATION && d->det_mode != QMC_DET_EXPLICIT) return QMC_ERR_ARG;
   if (d->precision != QMC_PREC_FP64 && d->precision != QMC_PREC_MIXED) return QMC_ERR_ARG;

@@ -538,6 +538,7 @@ int qmc_sweep_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void* stre
 
 bool qmc_sweep_eligible(const qmc_wf_desc* d, const qmc_metropolis_args* a) {
   return a->move_type != QMC_MOVE_ALL_ELEC && d->det_mode == QMC_DET_EXCITATION && d->ncfg == 1 &&
+         d->radial_type == QMC_RADIAL_GTO &&
          d->ndet[0] == 1 && d->ndet[1] == 1 && !a->psi_out && d->nup <= QMC_MAX_NSPIN &&
          d->ndown <= QMC_MAX_NSPIN;
 }

@@ -216,6 +216,66 @@ def huckel_mos(basis, atoms, atom_coords, k_wh=1.75):
     return mos, evals[: basis.nmo]
 
 
+# Minimal Slater-type basis ("slater-sz") with exponents from Slater's rules
+# (J. C. Slater, Phys. Rev. 36, 57 (1930)): zeta = (Z - s) / n with the
+# screening s of the rules; shells (n, l) per element, a 3d polarisation
+# shell (zeta 2.0) on second-row atoms. In the ADF layout the AO layer reads:
+# cartesian powers kx, ky, kz and the power of r, kr = n - 1 - l.
+SLATER_SZ = {
+    "H": [(1, 0, 1.0)],
+    "Li": [(1, 0, 2.70), (2, 0, 0.65), (2, 1, 0.65)],
+    "C": [(1, 0, 5.70), (2, 0, 1.625), (2, 1, 1.625), (3, 2, 2.0)],
+    "O": [(1, 0, 7.70), (2, 0, 2.275), (2, 1, 2.275), (3, 2, 2.0)],
+}
+
+
+def build_slater_namespace(atoms, atom_coords, seed=0):
+    """Basis namespace of the ADF calculator's layout (adf.py:205-275:
+    radial_type "sto", cartesian harmonics, one uncontracted entry per AO,
+    coefficients 1) for the "slater-sz" basis. No Slater-orbital integrals
+    are available here, so the MOs are seeded orthonormal columns (synthetic
+    inputs of the right shape), normalised as the reference does."""
+    from ..wavefunction.tables import norm_slater_cst
+    nshells, kx, ky, kz, kr, ex, bn, bl = [], [], [], [], [], [], [], []
+    for sym in atoms:
+        cnt = 0
+        for (n, lval, zeta) in SLATER_SZ[sym]:
+            for c in range(len(_KX[lval])):
+                kx.append(_KX[lval][c])
+                ky.append(_KY[lval][c])
+                kz.append(_KZ[lval][c])
+                kr.append(n - 1 - lval)
+                ex.append(zeta)
+                bn.append(n)
+                bl.append(lval)
+                cnt += 1
+        nshells.append(cnt)
+    nao = len(ex)
+    basis = SimpleNamespace()
+    basis.radial_type = "sto"
+    basis.harmonics_type = "cart"
+    basis.nao = nao
+    basis.nmo = nao
+    basis.nshells = nshells
+    basis.nao_per_atom = nshells
+    basis.index_ctr = np.arange(nao)
+    basis.nctr_per_ao = np.ones(nao, dtype=np.int64)
+    basis.bas_kx, basis.bas_ky, basis.bas_kz = (np.array(v) for v in (kx, ky, kz))
+    basis.bas_kr = np.array(kr)
+    basis.bas_exp = np.array(ex, dtype=np.float64)
+    basis.bas_coeffs = np.ones(nao)
+    basis.bas_n, basis.bas_l = bn, bl
+    basis.bas_m = [0] * nao
+    basis.bas_norm = norm_slater_cst(basis.bas_kx, basis.bas_ky, basis.bas_kz, basis.bas_kr,
+                                     basis.bas_exp)
+    basis.atom_coords_internal = np.asarray(atom_coords, dtype=np.float64)
+    q, _ = np.linalg.qr(np.random.default_rng(seed).normal(size=(nao, nao)))
+    basis.mos = q / np.sqrt((q ** 2).sum(0))
+    basis.mo_energy = np.arange(nao, dtype=np.float64)
+    basis.TotalEnergy = float("nan")
+    return basis
+
+
 _SCF_CACHE = {}
 
 
@@ -243,7 +303,9 @@ class Molecule:
 
     ``calculator``: ``"pyscf"`` (default, RHF orbitals as the reference's pyscf
     calculator provides them, computed by this package) or ``"huckel"`` /
-    ``"builtin"`` (extended-Hueckel guess); both on the built-in basis tables.
+    ``"builtin"`` (extended-Hueckel guess), both on the built-in Gaussian
+    tables; ``"slater"``: the minimal Slater-type basis "slater-sz" in the ADF
+    calculator's layout with synthetic orthonormal MOs.
     ``load`` accepts a ``.npz`` file written by :meth:`save`.
     """
 
@@ -267,8 +329,8 @@ class Molecule:
             return
         if unit not in ("angs", "bohr"):
             raise ValueError("unit should be angs or bohr")
-        if calculator not in ("pyscf", "builtin", "huckel"):
-            raise ValueError("calculator must be 'pyscf' (RHF) or 'huckel'")
+        if calculator not in ("pyscf", "builtin", "huckel", "slater"):
+            raise ValueError("calculator must be 'pyscf' (RHF), 'huckel' or 'slater'")
         for a in atom.split(";"):
             if not a.strip():
                 continue
@@ -292,6 +354,10 @@ class Molecule:
         if self.name is None:
             self.name = "".join(self.atoms)
         self.hdf5file = "_".join([self.name, calculator, basis]) + ".hdf5"
+        if calculator == "slater":
+            self.basis = build_slater_namespace(self.atoms, self.atom_coords)
+            self.atoms = np.array(self.atoms)
+            return
         self.basis = build_basis_namespace(self.atoms, self.atom_coords, basis)
         if calculator == "pyscf" and self.spin == 0:
             self.basis.mos, self.basis.mo_energy, self.basis.TotalEnergy = scf_orbitals(

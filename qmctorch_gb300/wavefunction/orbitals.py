@@ -15,12 +15,13 @@ from torch import nn
 
 from .. import _lib
 from . import runtime as rt
-from .tables import BasisTables, norm_cst
+from .tables import BasisTables, entry_norms
 
 
 class AtomicOrbitals(nn.Module):
-    """AO values, gradients and laplacians of cartesian GTOs
-    (atomic_orbitals.py:15-218)."""
+    """AO values, gradients and laplacians of cartesian Gaussian (pyscf
+    layout) or Slater-type (ADF layout: r^kr exp(-a r), or exp(-a r) for
+    radial_type "sto_pure") orbitals (atomic_orbitals.py:15-218)."""
 
     def __init__(self, mol, cuda=False):
         super().__init__()
@@ -42,8 +43,7 @@ class AtomicOrbitals(nn.Module):
         self.bas_exp.requires_grad = True
         self.harmonics_type = mol.basis.harmonics_type
         self.radial_type = mol.basis.radial_type
-        self.norm_cst = torch.as_tensor(norm_cst(mol.basis.bas_kx, mol.basis.bas_ky,
-                                                 mol.basis.bas_kz, mol.basis.bas_exp)).type(dtype)
+        self.norm_cst = torch.as_tensor(entry_norms(mol.basis)).type(dtype)
         self._basis = mol.basis
         self._tables = BasisTables(mol.basis, np.asarray(mol.basis.bas_exp, dtype=np.float64))
         self._tables_version = None

@@ -123,6 +123,8 @@ def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None
     d.gprim_entry, d.bas_exp, d.ao_k = ptr(t["gprim_entry"]), ptr(bexp), ptr(t["ao_k"])
     d.ao_wofs, d.ao_wd = ptr(t["ao_wofs"]), ptr(t["ao_wd"])
     d.weight_entry = ptr(t["w_entry"])
+    d.radial_type = int(bt.radial)
+    d.ao_kr = ptr(t["ao_kr"])
     d.ao_wv = ptr(t["ao_wv"]) if not bt.contract else None
     if mo is not None:
         scf = dev64(mo.mo_scf, device)

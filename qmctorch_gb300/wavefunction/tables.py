@@ -17,6 +17,7 @@ excitation for the spin-down double indices, line 186) and
 """
 from __future__ import annotations
 
+import math
 from itertools import combinations, product
 
 import numpy as np
@@ -39,14 +40,51 @@ def norm_cst(bas_kx, bas_ky, bas_kz, bas_exp):
     return out
 
 
+def _dfact(n):
+    out = 1
+    for k in range(int(n), 0, -2):
+        out *= k
+    return out
+
+
+def norm_slater_cst(bas_kx, bas_ky, bas_kz, bas_kr, bas_exp):
+    """Per-entry norm of a cartesian STO x^a y^b z^c r^n exp(-alpha r)
+    (``norm_slater_cartesian``, norm_orbital.py:106-161): with
+    L = a + b + c + n + 1, 1 / sqrt(4 pi (2L)! / (2 alpha)^(2L + 1)
+    (2a-1)!! (2b-1)!! (2c-1)!! / (2a + 2b + 2c + 1)!!)."""
+    a, b, c = (np.asarray(v, dtype=np.int64) for v in (bas_kx, bas_ky, bas_kz))
+    n = np.asarray(bas_kr, dtype=np.float64)
+    alpha = np.asarray(bas_exp, dtype=np.float64)
+    lv = a + b + c + n + 1.0
+    lfact = np.array([float(math.factorial(int(2 * v))) for v in lv])
+    pref = 4.0 * np.pi * lfact / (2.0 * alpha) ** (2.0 * lv + 1.0)
+    num = np.array([float(_dfact(2 * x - 1) * _dfact(2 * y - 1) * _dfact(2 * z - 1))
+                    for x, y, z in zip(a, b, c)])
+    den = np.array([float(_dfact(2 * x + 2 * y + 2 * z + 1)) for x, y, z in zip(a, b, c)])
+    return np.sqrt(1.0 / (pref * num / den))
+
+
+RADIAL = {"gto": 0, "gto_pure": 0, "sto": 1, "sto_pure": 2}
+
+
+def entry_norms(basis):
+    """The AO layer's per-entry norms (atomic_orbital_norm, norm_orbital.py:8-47)
+    for the cartesian radial types this package evaluates."""
+    if str(basis.radial_type).startswith("sto"):
+        kr = getattr(basis, "bas_kr", np.zeros(len(basis.bas_exp)))
+        return norm_slater_cst(basis.bas_kx, basis.bas_ky, basis.bas_kz, kr, basis.bas_exp)
+    return norm_cst(basis.bas_kx, basis.bas_ky, basis.bas_kz, basis.bas_exp)
+
+
 class BasisTables:
     """AO group tables built from the namespace and the current exponents."""
 
     def __init__(self, basis, bas_exp_values):
-        if basis.harmonics_type != "cart" or not str(basis.radial_type).startswith("gto"):
+        if basis.harmonics_type != "cart" or str(basis.radial_type) not in RADIAL:
             raise NotImplementedError(
-                "the GB300 AO kernel evaluates cartesian GTOs (radial_type 'gto_pure', "
-                "harmonics_type 'cart'), the layout of the pyscf calculator")
+                "the GB300 AO kernels evaluate cartesian harmonics with Gaussian (pyscf layout) "
+                "or Slater (ADF layout) radial functions")
+        self.radial = RADIAL[str(basis.radial_type)]
         self.nao = int(basis.nao)
         index_ctr = np.asarray(basis.index_ctr, dtype=np.int64)
         nshells = np.asarray(basis.nshells, dtype=np.int64)
@@ -54,7 +92,10 @@ class BasisTables:
         kxyz = np.stack([np.asarray(basis.bas_kx), np.asarray(basis.bas_ky),
                          np.asarray(basis.bas_kz)], axis=1).astype(np.int64)
         coeffs = np.asarray(basis.bas_coeffs, dtype=np.float64)
-        norm = norm_cst(basis.bas_kx, basis.bas_ky, basis.bas_kz, basis.bas_exp)
+        norm = entry_norms(basis)
+        kr = np.asarray(getattr(basis, "bas_kr", np.zeros(len(index_ctr))), dtype=np.int64)
+        if self.radial != 1:
+            kr = np.zeros_like(kr)
         self.contract = len(np.unique(index_ctr)) != len(index_ctr)
         exps = np.asarray(bas_exp_values, dtype=np.float64)
         # entries of each AO, in namespace order
@@ -63,15 +104,18 @@ class BasisTables:
             ao_entries[a].append(e)
         ao_atom = np.zeros(self.nao, dtype=np.int64)
         ao_k = np.zeros((self.nao, 3), dtype=np.int64)
+        ao_kr = np.zeros(self.nao, dtype=np.int64)
         for a, ents in enumerate(ao_entries):
             if not ents:
                 raise ValueError("AO %d has no primitive" % a)
             at = set(entry_atom[ents].tolist())
             ks = {tuple(kxyz[e]) for e in ents}
-            if len(at) != 1 or len(ks) != 1:
-                raise NotImplementedError("AO %d mixes atoms or cartesian powers" % a)
+            krs = {int(kr[e]) for e in ents}
+            if len(at) != 1 or len(ks) != 1 or len(krs) != 1:
+                raise NotImplementedError("AO %d mixes atoms or powers" % a)
             ao_atom[a] = at.pop()
             ao_k[a] = ks.pop()
+            ao_kr[a] = krs.pop()
         # group consecutive AOs with identical exponent lists on the same atom
         groups = []
         a = 0
@@ -79,7 +123,7 @@ class BasisTables:
             key = exps[ao_entries[a]].tobytes()
             b = a + 1
             while (b < self.nao and b - a < MAX_COMP and ao_atom[b] == ao_atom[a]
-                   and exps[ao_entries[b]].tobytes() == key):
+                   and exps[ao_entries[b]].tobytes() == key and ao_kr[b] == ao_kr[a]):
                 b += 1
             groups.append((a, b))
             a = b
@@ -107,7 +151,7 @@ class BasisTables:
             "group_atom": i32(group_atom), "group_prim": i32(group_prim),
             "group_ao": i32(group_ao), "gprim_entry": i32(gprim_entry),
             "ao_k": i32(ao_k.reshape(-1)), "ao_wofs": i32(ao_wofs), "ao_wd": f64(wd),
-            "ao_wv": f64(wv), "w_entry": i32(w_entry),
+            "ao_wv": f64(wv), "w_entry": i32(w_entry), "ao_kr": i32(ao_kr),
         }
         self.ngroup = len(groups)
         self.ngprim = len(gprim_entry)

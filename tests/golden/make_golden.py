@@ -70,6 +70,19 @@ CASES.update({
 })
 
 
+# Slater-type orbital cases: the "slater-sz" basis in the ADF calculator's
+# layout (radial_type "sto", cartesian harmonics, kr powers of r).
+CASES.update({
+    "lih_sto": ("Li 0 0 0; H 0 0 1.595", "angs", "slater-sz", "cas(2,2)", True, 10, True,
+                ("metropolis", "solver")),
+    "h2o_sto": ("O 0 0 0.1173; H 0 0.7572 -0.4692; H 0 -0.7572 -0.4692", "angs", "slater-sz",
+                "single_double(2,2)", True, 8, True, ("metropolis", "solver")),
+})
+# MO source of each case: the fixtures of Gaussian bases were written with
+# the extended-Hueckel orbitals, those of the Slater basis with its synthetic ones
+CALCULATOR = {"lih_sto": "slater", "h2o_sto": "slater"}
+
+
 def make_jastrow(mol, name):
     """The reference Jastrow object of a case (None: the default e-e factor)."""
     if name not in JASTROW:
@@ -112,7 +125,7 @@ def main(reference_root, only=()):
         if only and name not in only:
             continue
         torch.manual_seed(1234)
-        mol = Molecule(atoms, unit=unit, basis=basis)
+        mol = Molecule(atoms, unit=unit, basis=basis, calculator=CALCULATOR.get(name, "huckel"))
         tmp = os.path.join(HERE, "_tmp_mol.npz")
         mol.save(tmp)
         data = dict(np.load(tmp))
@@ -292,7 +305,7 @@ def make_gmetropolis(reference_root):
     from qmctorch_gb300.scf import Molecule
     atoms, unit, basis, configs, all_mo = CASES["h2"][:5]
     torch.manual_seed(1234)
-    mol = Molecule(atoms, unit=unit, basis=basis)
+    mol = Molecule(atoms, unit=unit, basis=basis, calculator="huckel")
     wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)
     h2pos0 = seeded_positions(mol, 16, seed=21)
     hs = GeneralizedMetropolis(nwalkers=16, nstep=20, step_size=0.2, ntherm=-10, ndecor=2,
@@ -328,7 +341,7 @@ def make_walkers(reference_root):
     out = {}
     for name in WALKER_CASES:
         atoms, unit, basis = CASES[name][:3]
-        mol = Molecule(atoms, unit=unit, basis=basis)
+        mol = Molecule(atoms, unit=unit, basis=basis, calculator="huckel")
         for method in WALKER_METHODS:
             torch.manual_seed(WALKER_SEEDS[0])
             np.random.seed(WALKER_SEEDS[1])
@@ -415,7 +428,7 @@ def make_hamiltonian(reference_root):
     samples = s(pdf, pos=torch.as_tensor(pos0), with_tqdm=False)
     atoms, unit, basis, configs, all_mo = CASES["h2"][:5]
     torch.manual_seed(1234)
-    mol = Molecule(atoms, unit=unit, basis=basis)
+    mol = Molecule(atoms, unit=unit, basis=basis, calculator="huckel")
     wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)
     h2pos0 = seeded_positions(mol, g["nwalkers"], seed=31)
     s2 = sampler()
@@ -442,7 +455,7 @@ def make_fp32(reference_root):
 
     atoms, unit, basis, configs, all_mo, nw = CASES["lih_cas"][:6]
     torch.manual_seed(1234)
-    mol = Molecule(atoms, unit=unit, basis=basis)
+    mol = Molecule(atoms, unit=unit, basis=basis, calculator="huckel")
     set_torch_single_precision()
     try:
         wf = SlaterJastrow(mol, configs=configs, include_all_mo=all_mo)

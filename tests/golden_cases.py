@@ -2,7 +2,7 @@
 
 ``CASES`` use the default e-e Pade Jastrow; ``EN_CASES`` use the
 electron-nucleus Pade factor, alone ("en") or combined with the e-e factor
-("ee+en", CombineJastrow)."""
+("ee+en", CombineJastrow); ``STO_CASES`` use Slater-type orbitals."""
 import os
 
 import numpy as np
@@ -12,6 +12,8 @@ from qmctorch_gb300.scf import Molecule
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 CASES = ["h2", "lih_cas", "lih_sd", "h2o_sd", "h2o_single", "h4", "c6h6"]
 EN_CASES = ["h2_en", "lih_en", "h2o_en", "c6h6_en"]
+# Slater-type orbitals in the ADF layout (radial_type "sto", cartesian harmonics)
+STO_CASES = ["lih_sto", "h2o_sto"]
 
 _EE = "jastrow.jastrow_terms.0.jastrow_kernel.weight"
 _EN = "jastrow.jastrow_terms.1.jastrow_kernel.weight"

@@ -4,9 +4,9 @@ import numpy as np
 import pytest
 
 from oracle import qmc_oracle as orc
-from tests.golden_cases import CASES, EN_CASES, jastrow_weights, load
+from tests.golden_cases import CASES, EN_CASES, STO_CASES, jastrow_weights, load
 
-ALL = CASES + EN_CASES
+ALL = CASES + EN_CASES + STO_CASES
 
 RTOL = 1e-10
 
