@@ -10,6 +10,7 @@ part of this package's dependencies).
 from __future__ import annotations
 
 import logging
+import os
 import time
 from types import SimpleNamespace
 
@@ -45,6 +46,21 @@ class SolverBase:
         self.hdf5file = output
         if output is None:
             self.hdf5file = str(getattr(self.wf.mol, "name", "qmc")) + "_QMCTorch.hdf5"
+        # observables go to an .npz archive with the HDF5 file's tree
+        # (utils/observable_store.py) when the caller names the output file
+        self.dump_file = None
+        if output is not None:
+            self.dump_file = os.path.splitext(str(output))[0] + ".npz"
+
+    def _dump(self, obs, group, kind):
+        """solver_base.py:384-385 / solver.py:262-264: the observables of a
+        calculation under ``group`` with its type attribute."""
+        if self.dump_file is None:
+            return group
+        from ..utils import add_group_attr, dump_observables
+        group = dump_observables(obs, self.dump_file, root_name=group)
+        add_group_attr(self.dump_file, group, {"type": kind})
+        return group
 
     def configure_resampling(self, mode="update", resample_every=1, nstep_update=25,
                              ntherm_update=-1, increment={"every": None, "factor": None}):
@@ -135,7 +151,9 @@ class SolverBase:
         log.info("  Energy   : %f +/- %f", e.item(), err.item())
         log.info("  Variance : %f", s.item())
         log.info("  Size     : %d", len(eloc))
-        return SimpleNamespace(pos=pos, local_energy=eloc, energy=e, variance=s, error=err)
+        obs = SimpleNamespace(pos=pos, local_energy=eloc, energy=e, variance=s, error=err)
+        self._dump(obs, hdf5_group, "single_point")
+        return obs
 
     def sampling_traj(self, pos=None, with_tqdm=True, hdf5_group="sampling_trajectory"):
         """Local energies along a sampling trajectory (solver_base.py:435-471):
@@ -151,7 +169,9 @@ class SolverBase:
             if self.wf.cuda and flat.device.type == "cpu":
                 flat = flat.to(self.device)
             el = self.wf.local_energy(flat).reshape(-1, nw).cpu().numpy()
-        return SimpleNamespace(local_energy=el, pos=pos)
+        obs = SimpleNamespace(local_energy=el, pos=pos)
+        self._dump(obs, hdf5_group, "sampling_traj")
+        return obs
 
     def print_parameters(self, grad=False):
         """Print the trainable parameters, or their gradients (solver_base.py:473-484)."""
@@ -257,6 +277,7 @@ class Solver(SolverBase):
         self.run_epochs(nepoch)
         self.restore_sampling_parameters()
         self.observable.models.last = dict(self.wf.state_dict())
+        self._dump(self.observable, hdf5_group, "opt")
         return self.observable
 
     def prepare_optimization(self, batchsize, chkpt_every, tqdm=False):

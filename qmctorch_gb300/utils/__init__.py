@@ -43,4 +43,7 @@ class DataLoader:
         raise StopIteration
 
 
-__all__ = ["set_torch_double_precision", "set_torch_single_precision", "DataLoader"]
+from .observable_store import add_group_attr, dump_observables, load_observables  # noqa: E402
+
+__all__ = ["set_torch_double_precision", "set_torch_single_precision", "DataLoader",
+           "dump_observables", "add_group_attr", "load_observables"]

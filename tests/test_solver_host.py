@@ -60,3 +60,26 @@ def test_optimization_step_passes_positions_only_when_needed():
         lpos = torch.zeros(2, 6)
         solver.optimization_step(lpos)
         assert len(opt.args) == expect
+
+
+def test_observable_store_keeps_the_hdf5_tree(tmp_path):
+    """dump_observables / add_group_attr / load_observables: the tree of the
+    reference's HDF5 dump (hdf5_utils.py:130-160) in an .npz archive, with the
+    "_<n>" suffix for a root name already present."""
+    from types import SimpleNamespace
+
+    import numpy as np
+    import torch
+
+    from qmctorch_gb300.utils import add_group_attr, dump_observables, load_observables
+    f = str(tmp_path / "obs.npz")
+    obs = SimpleNamespace(energy=[1.0, 2.0, 3.0], local_energy=torch.arange(4.0),
+                          models=SimpleNamespace(last={"w": torch.ones(2)}))
+    assert dump_observables(obs, f, "wf_opt") == "wf_opt"
+    add_group_attr(f, "wf_opt", {"type": "opt"})
+    assert dump_observables(obs, f, "wf_opt") == "wf_opt_2"
+    back = load_observables(f, "wf_opt")
+    np.testing.assert_array_equal(back.energy, [1.0, 2.0, 3.0])
+    np.testing.assert_array_equal(back.local_energy, [0, 1, 2, 3])
+    np.testing.assert_array_equal(back.models.last.w, [1.0, 1.0])
+    assert str(back.attrs["type"]) == "opt"
