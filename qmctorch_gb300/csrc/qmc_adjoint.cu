@@ -210,7 +210,7 @@ __global__ void __launch_bounds__(kAdjTPB) psi_adjoint_kernel(
             double dao;
             if (t.radial != QMC_RADIAL_GTO)  // Slater type: d/d alpha r^n e^(-alpha r)
               dao = vs * t.wd[wi] *
-                    sto_dalpha(pl.p, 0.0, 0.0, 0.0, 0.0, 0, dx, dy, dz, r2, t.ao_kr[a],
+                    sto_dalpha(pl.p, 0.0, 0.0, 0.0, 0.0, 0, dx, dy, dz, r2, t.ao_kr(a),
                                t.walpha[wi]).v;
             else
               dao = -vs * t.wd[wi] * pl.p * r2 * exp(-t.walpha[wi] * r2);
@@ -543,7 +543,7 @@ __global__ void __launch_bounds__(kAdjTPB) eloc_adjoint_kernel(
             double dval, dgx, dgy, dgz, dlap;
             if (t.radial != QMC_RADIAL_GTO) {  // Slater type
               const StoDAlpha sd = sto_dalpha(pl.p, pl.dx, pl.dy, pl.dz, pl.lap, l, dx, dy, dz,
-                                              r2, t.ao_kr[a], al);
+                                              r2, t.ao_kr(a), al);
               dval = vs * wp * sd.v;
               dgx = wp * sd.gx;
               dgy = wp * sd.gy;

@@ -369,7 +369,7 @@ __device__ __forceinline__ void group_sto(const Tables<R>& t, int g, R dx, R dy,
       const int wi = t.ao_wofs[a] + p;
       const R wg = t.wd[wi];
       const AOVal<R> q = sto_from<R, DERIV>(px * py * pz, qx, qy, qz, lapP, kx + ky + kz, dx, dy,
-                                            dz, r2, t.ao_kr[a], t.walpha[wi], vs * wg, wg);
+                                            dz, r2, t.ao_kr(a), t.walpha[wi], vs * wg, wg);
       o.v += q.v;
       if (DERIV) {
         o.gx += q.gx;
@@ -949,7 +949,7 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
     const int spin = tid / nwb, wl = tid - spin * nwb;
     if (w0 + wl < nw)
       ep_det<R, KIN>(d, L, dbase, dss, dsm ? wl : w0 + wl, spin, MO, BK, wl, nwb, DREF,
-                     t.det_tab[spin]);
+                     d.det_table[spin]);
   }
   __syncthreads();
   if (tid < nwb && w0 + tid < nw) {
@@ -960,8 +960,7 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
     const int64_t slot = dsm ? wl : w;
     const T* dv = rptr<T>(dbase, L.dv, dss, slot);
     const double* ov = KIN ? rptr<double>(dbase, L.ov, dss, slot) : nullptr;
-    const double psid = ci_combine<T, KIN, T>(d, t.cfg_det[0], t.cfg_det[1], t.ci_w, dv, ov, dss,
-                                              DREF[wl], DREF[nwb + wl], &kin);
+    const double psid = ci_combine<T, KIN, T>(d, dv, ov, dss, DREF[wl], DREF[nwb + wl], &kin);
     double logj = 0.0, v = 0.0;
     for (int e = 0; e < ne; ++e) {
       logj += JR[e * nwb + wl];

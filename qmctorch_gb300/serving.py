@@ -57,12 +57,17 @@ MAX_BATCH = 32  # QMC_MAX_BATCH of qmc_metropolis_run_batch
 @dataclass
 class Request:
     """One VMC single point: ``atoms`` (``Molecule`` syntax), ``nwalkers``
-    walkers, ``nstep`` all-electron Metropolis steps of ``step_size``."""
+    walkers, ``nstep`` all-electron Metropolis steps of ``step_size``.
+    ``calculator``: the molecular orbitals (``Molecule``): the extended-Hueckel
+    guess by default -- an SCF per request on the scheduler's host thread
+    would hold every other request while it runs -- or "pyscf" for this
+    package's RHF."""
     atoms: str
     nwalkers: int
     nstep: int
     unit: str = "angs"
     basis: str = "sto-3g"
+    calculator: str = "huckel"
     configs: str = "ground_state"
     step_size: float = 0.2
     seed: int = 0
@@ -266,9 +271,10 @@ class GPUExecutor:
 
     def _molecule(self, req):
         from .scf import Molecule
-        k = (req.atoms, req.unit, req.basis)
+        k = (req.atoms, req.unit, req.basis, req.calculator)
         if k not in self._mols:
-            self._mols[k] = Molecule(req.atoms, unit=req.unit, basis=req.basis)
+            self._mols[k] = Molecule(req.atoms, unit=req.unit, basis=req.basis,
+                                     calculator=req.calculator)
             if len(self._mols) > 4096:
                 self._mols.clear()
         return self._mols[k]

@@ -24,7 +24,7 @@ pytestmark = pytest.mark.gpu
 def _mol(n, spacing):
     from qmctorch_gb300.scf import Molecule
     from qmctorch_gb300.serving import hydrogen_chain
-    return Molecule(hydrogen_chain(n, spacing), unit="angs", basis="sto-3g")
+    return Molecule(hydrogen_chain(n, spacing), unit="angs", basis="sto-3g", calculator="huckel")
 
 
 def _wf(mol, precision="mixed"):
