@@ -168,6 +168,17 @@ template <typename R>
 struct EPBound {
   static constexpr int kThreads = kMixed<R> ? 1024 : 512;
 };
+// The FP32 local-energy kernel (electron phase with gradient and laplacian
+// accumulators, determinant phase in registers) is bounded at 640 threads:
+// 96 registers, and still 4 blocks of 32 x 5 threads per SM.
+template <typename R>
+struct EPElBound {
+  static constexpr int kThreads = kMixed<R> ? 640 : 512;
+};
+template <typename R>
+__host__ __device__ constexpr int ep_thread_bound(int kind) {
+  return kind == 1 ? EPElBound<R>::kThreads : EPBound<R>::kThreads;
+}
 
 
 // ---------------------------------------------------------------------------
@@ -707,12 +718,12 @@ template <typename R, int N>
 __device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> mo, CView<R> bk,
                                        int nv, const int* tab, double* dv, double* ov, int64_t s,
                                        double* dref) {
-  constexpr int NC = N + kElRegNV;
-  R a[N][NC];
+  // LU of the occupied block (lu_factor's operations and pivots)
+  R a[N][N];
 #pragma unroll
   for (int i = 0; i < N; ++i)
 #pragma unroll
-    for (int j = 0; j < NC; ++j) a[i][j] = (j < N + nv) ? mo(i, j) : (R)0;
+    for (int j = 0; j < N; ++j) a[i][j] = mo(i, j);
   int piv[N];
   double det = 1.0;
 #pragma unroll
@@ -732,7 +743,7 @@ __device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> 
     for (int i = k + 1; i < N; ++i) {
       const bool sw = (i == p);
 #pragma unroll
-      for (int j = 0; j < NC; ++j) {
+      for (int j = 0; j < N; ++j) {
         const R x = a[k][j], y = a[i][j];
         a[k][j] = sw ? y : x;
         a[i][j] = sw ? x : y;
@@ -752,36 +763,34 @@ __device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> 
     }
   }
   *dref = det;
-  // residual of a solve x of column b (b in the original row order), corrected
-  // with the FP32 factors, in FP64 (lu_refine)
-  auto refine = [&](const R (&b)[N], const R (&x)[N], double (&x64)[N]) {
+  // x = A^-1 b of column c of the MO (kin = false) or kinetic (kin = true)
+  // rows, with one FP64 refinement step (lu_solve, then lu_refine)
+  auto solve = [&](bool kin, int c, double (&x64)[N]) {
+    R x[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) x[i] = kin ? bk(i, c) : mo(i, c);
+    apply_pivots<R, N>(piv, x);
+    lu_subst<R, N, N>(a, x);
     R rc[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      double r = (double)b[i];
+      double r = (double)(kin ? bk(i, c) : mo(i, c));
 #pragma unroll
       for (int k = 0; k < N; ++k) r = fma(-(double)mo(i, k), (double)x[k], r);
       rc[i] = (R)r;
     }
     apply_pivots<R, N>(piv, rc);
-    lu_subst<R, N, NC>(a, rc);
+    lu_subst<R, N, N>(a, rc);
 #pragma unroll
     for (int i = 0; i < N; ++i) x64[i] = (double)x[i] + (double)rc[i];
   };
-  // X = A^-1 A_virt (the virtual columns were interchanged with the rows)
+  // X = A^-1 A_virt, refined
   double x64[N][kElRegNV];
 #pragma unroll
   for (int c = 0; c < kElRegNV; ++c) {
     if (c >= nv) break;
-    R x[N], b[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) {
-      x[i] = a[i][N + c];
-      b[i] = mo(i, N + c);
-    }
-    lu_subst<R, N, NC>(a, x);
     double y[N];
-    refine(b, x, y);
+    solve(false, N + c, y);
 #pragma unroll
     for (int i = 0; i < N; ++i) x64[i][c] = y[i];
   }
@@ -794,13 +803,8 @@ __device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> 
   for (int cc = 0; cc < N + kElRegNV; ++cc) {
     const int c = cc < kElRegNV ? N + cc : cc - kElRegNV;  // virtual, then occupied
     if (cc < kElRegNV && cc >= nv) continue;
-    R b[N], x[N];
-#pragma unroll
-    for (int i = 0; i < N; ++i) b[i] = x[i] = bk(i, c);
-    apply_pivots<R, N>(piv, x);
-    lu_subst<R, N, NC>(a, x);
     double y[N];
-    refine(b, x, y);
+    solve(true, c, y);
     if (cc < kElRegNV) {
 #pragma unroll
       for (int i = 0; i < N; ++i) m64[i][cc] = y[i];

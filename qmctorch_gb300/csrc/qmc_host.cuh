@@ -128,7 +128,7 @@ static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, 
       const int nslot = (ne + k - 1) / k;
       if (k > 1 && nslot == (ne + k - 2) / (k - 1)) continue;  // same slot count as k - 1
       const EPShape s = ep_shape<R>(d, kind, nwb, jc, nslot);
-      if (s.nthreads > EPBound<R>::kThreads || s.smem > 200 * 1024) continue;
+      if (s.nthreads > ep_thread_bound<R>(kind) || s.smem > 200 * 1024) continue;
       if (prepare_smem(kernel, s.smem) != QMC_OK) continue;
       int occ = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, s.nthreads, s.smem) !=

@@ -29,7 +29,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_psi_kernel(const qmc_
 }
 
 template <typename R, int JC>
-__global__ void __launch_bounds__(EPBound<R>::kThreads) ep_eloc_kernel(const qmc_wf_desc d, const double* __restrict__ pos,
+__global__ void __launch_bounds__(EPElBound<R>::kThreads) ep_eloc_kernel(const qmc_wf_desc d, const double* __restrict__ pos,
                                                        int64_t nw, double* __restrict__ eloc,
                                                        double* __restrict__ kin,
                                                        double* __restrict__ psi,
@@ -52,8 +52,9 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_eloc_kernel(const qmc
 }
 
 template <typename R, typename K>
-static int launch_prepare(K kernel, const EPShape& S) {
-  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > EPBound<R>::kThreads) return QMC_ERR_SHAPE;
+static int launch_prepare(K kernel, const EPShape& S, int kind) {
+  if (S.smem < 0 || S.smem > 227 * 1024 || S.nthreads > ep_thread_bound<R>(kind))
+    return QMC_ERR_SHAPE;
   return prepare_smem(kernel, S.smem);
 }
 
@@ -61,7 +62,7 @@ template <typename R, int JC>
 static int launch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, double* psi,
                       unsigned char* scr, cudaStream_t s) {
   const EPShape S = ep_plan<R>(*d, 0, JC, ep_psi_kernel<R, JC>, nw);
-  int st = launch_prepare<R>(ep_psi_kernel<R, JC>, S);
+  int st = launch_prepare<R>(ep_psi_kernel<R, JC>, S, 0);
   if (st) return st;
   const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
   ep_psi_kernel<R, JC><<<grid, S.nthreads, S.smem, s>>>(*d, pos, nw, psi, scr, pad_walkers(nw), S);
@@ -80,7 +81,7 @@ template <typename R, int JC>
 static int launch_eloc(const qmc_wf_desc* d, const double* pos, int64_t nw, double* eloc,
                        double* kin, double* psi, unsigned char* scr, cudaStream_t s) {
   const EPShape S = ep_plan<R>(*d, 1, JC, ep_eloc_kernel<R, JC>, nw);
-  int st = launch_prepare<R>(ep_eloc_kernel<R, JC>, S);
+  int st = launch_prepare<R>(ep_eloc_kernel<R, JC>, S, 1);
   if (st) return st;
   const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
   ep_eloc_kernel<R, JC><<<grid, S.nthreads, S.smem, s>>>(*d, pos, nw, eloc, kin, psi, scr,
