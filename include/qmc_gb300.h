@@ -355,8 +355,20 @@ typedef struct qmc_metropolis_args {
   const int32_t* electron_index;
 } qmc_metropolis_args;
 
-/* Scratch bytes for qmc_metropolis_run. */
+/* Scratch bytes for qmc_metropolis_run: the determinant work arrays and room
+   for the walkers' current positions (launch plans that keep them out of
+   shared memory). */
 int64_t qmc_metropolis_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
+
+/*
+ * Launch plan of the all-electron Metropolis kernel for nwalkers walkers
+ * (diagnostics, no counterpart in the reference): plan[0] walkers per block,
+ * plan[1] threads per walker, plan[2] threads per block, plan[3] 1 when the
+ * current positions live in the scratch instead of shared memory (no plan
+ * with them in shared memory runs in one wave), plan[4] dynamic shared
+ * memory bytes per block. Needs a CUDA device (occupancy query).
+ */
+int qmc_metropolis_plan(const qmc_wf_desc* d, int64_t nwalkers, int32_t* plan);
 
 /*
  * Run nstep Metropolis steps for every walker in one persistent launch.

@@ -132,6 +132,7 @@ SIGNATURES = {
     "qmc_status_string": (ctypes.c_char_p, [ctypes.c_int]),
     "qmc_scratch_bytes": (c_int64, [_P(WfDesc), c_int64, c_int32]),
     "qmc_metropolis_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
+    "qmc_metropolis_plan": (ctypes.c_int, [_P(WfDesc), c_int64, _P(c_int32)]),
     "qmc_wf_psi": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p, c_int64,
                                   c_void_p]),
     "qmc_wf_psi_static": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_void_p, c_void_p]),

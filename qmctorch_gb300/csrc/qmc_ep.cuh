@@ -99,6 +99,8 @@ struct EPShape {
   int ncol;      // W columns stored per AO (nmo_used rounded up to the MO chunk)
   int pstride;   // split coordinates per walker row of the position arrays: 3 nelec made
                  // odd, so that the 32 walkers of a warp read distinct banks
+  int pos_global;  // Metropolis: the current positions live in the HBM scratch (after the
+                   // determinant work arrays, [coordinate][walker]) instead of shared memory
   int64_t smem;  // dynamic shared memory bytes
   int64_t o_tab, o_pos, o_pnew, o_mo, o_bk, o_jrow, o_vrow, o_dref, o_psi, o_f, o_kin, o_v,
       o_iel, o_acc;
@@ -107,10 +109,11 @@ struct EPShape {
 
 template <typename R>
 __host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int nwb, int jc,
-                                           int nslot) {
+                                           int nslot, bool pos_global = false) {
   EPShape s;
   s.nwb = nwb;
   s.nslot = nslot;
+  s.pos_global = (kind == 2 && pos_global) ? 1 : 0;
   int nt = nwb * nslot;
   if (nt < 2 * nwb) nt = 2 * nwb;
   s.nthreads = ((nt + 31) / 32) * 32;
@@ -123,7 +126,7 @@ __host__ __device__ inline EPShape ep_shape(const qmc_wf_desc& d, int kind, int 
   o = (o + 15) & ~int64_t(15);
   s.pstride = (int)(nc | 1);
   s.o_pos = o;
-  o += align8(nwb * s.pstride * xps);
+  if (!s.pos_global) o += align8(nwb * s.pstride * xps);
   s.o_pnew = o;
   if (kind == 2) o += align8(nwb * s.pstride * xps);
   s.o_mo = o;

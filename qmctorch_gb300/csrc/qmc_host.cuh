@@ -60,6 +60,9 @@ static inline int prepare_smem(K kernel, int64_t bytes) {
 // staged pooling kernel (one thread per walker, FP64).
 static inline int64_t scratch_slot_bytes(const qmc_wf_desc* d, int kind) {
   int64_t b = ep_layout(*d, kind == 2 ? 0 : kind).bytes_per_slot;
+  // Metropolis: room for the walkers' current positions as split coordinates
+  // (launch plans with pos_global)
+  if (kind == 2) b += 3 * (int64_t)d->nelec * (d->precision == QMC_PREC_MIXED ? 8 : 16);
   if (kind == 1) {
     qmc_wf_desc dd = *d;
     dd.precision = QMC_PREC_FP64;
@@ -111,14 +114,19 @@ static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, 
       if (kv.first == key) return kv.second;
   }
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  int nwb = kMixed<R> ? 32 : 16;
-  while (nwb > 8 && (nw + nwb - 1) / nwb < nsm) nwb /= 2;
+  int nwb0 = kMixed<R> ? 32 : 16;
+  while (nwb0 > 8 && (nw + nwb0 - 1) / nwb0 < nsm) nwb0 /= 2;
   const int kmax = (kind == 1 && !kMixed<R>) ? 1 : 8;
   EPShape best = s1;
   best.smem = -1;  // nothing fits yet
   double best_fill = -1.0;
   bool one_wave = false;
-  for (; nwb >= 1 && !one_wave; nwb /= 2) {
+  // The Metropolis kernel keeps the current positions in shared memory; when
+  // no plan gives one wave that way, a second pass moves them to the
+  // (L2-resident) scratch, read once per step by the proposal and written on
+  // acceptance, which frees a position row per walker of shared memory.
+  for (int pg = 0; pg < (kind == 2 ? 2 : 1) && !one_wave; ++pg)
+  for (int nwb = nwb0; nwb >= 1 && !one_wave; nwb /= 2) {
     // the first block size that fits is kept, except by the persistent
     // Metropolis kernel (kind 2), which halves it down to 8 walkers while no
     // thread split gives a single wave (a partial last wave would run alone
@@ -127,7 +135,7 @@ static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, 
     for (int k = 1; k <= kmax; ++k) {
       const int nslot = (ne + k - 1) / k;
       if (k > 1 && nslot == (ne + k - 2) / (k - 1)) continue;  // same slot count as k - 1
-      const EPShape s = ep_shape<R>(d, kind, nwb, jc, nslot);
+      const EPShape s = ep_shape<R>(d, kind, nwb, jc, nslot, pg == 1);
       if (s.nthreads > ep_thread_bound<R>(kind) || s.smem > 200 * 1024) continue;
       if (prepare_smem(kernel, s.smem) != QMC_OK) continue;
       int occ = 0;

@@ -11,7 +11,8 @@ namespace qmc {
                                                unsigned char*, cudaStream_t);                  \
   extern template int launch_metropolis_batch<R, JC>(const qmc_wf_desc*,                       \
                                                      const qmc_metropolis_args*, void* const*, \
-                                                     int, cudaStream_t);
+                                                     int, cudaStream_t);                  \
+  extern template int plan_metropolis<R, JC>(const qmc_wf_desc*, int64_t, int32_t*);
 QMC_MET_EXTERN(float, 8)
 QMC_MET_EXTERN(float, 16)
 QMC_MET_EXTERN(float, 24)
@@ -56,6 +57,20 @@ int qmc_metropolis_run(const qmc_wf_desc* d, const qmc_metropolis_args* a, void*
   if (d->nmo_used <= 8) return launch_metropolis<double, 8>(d, a, scr, s);
   if (d->nmo_used <= 16) return launch_metropolis<double, 16>(d, a, scr, s);
   return launch_metropolis<double, 24>(d, a, scr, s);
+}
+
+int qmc_metropolis_plan(const qmc_wf_desc* d, int64_t nwalkers, int32_t* plan) {
+  int st = check_desc(d);
+  if (st) return st;
+  if (!plan || nwalkers < 1) return QMC_ERR_ARG;
+  if (d->precision == QMC_PREC_MIXED) {
+    if (d->nmo_used <= 8) return plan_metropolis<float, 8>(d, nwalkers, plan);
+    if (d->nmo_used <= 16) return plan_metropolis<float, 16>(d, nwalkers, plan);
+    return plan_metropolis<float, 24>(d, nwalkers, plan);
+  }
+  if (d->nmo_used <= 8) return plan_metropolis<double, 8>(d, nwalkers, plan);
+  if (d->nmo_used <= 16) return plan_metropolis<double, 16>(d, nwalkers, plan);
+  return plan_metropolis<double, 24>(d, nwalkers, plan);
 }
 
 int qmc_metropolis_run_batch(const qmc_wf_desc* descs, const qmc_metropolis_args* args,

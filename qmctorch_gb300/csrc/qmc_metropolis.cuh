@@ -37,16 +37,34 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
   const int64_t w = w0 + wl;
   const bool active = slot < nslot;    // an electron slot (electrons slot, slot + nslot, ...)
   const bool live = active && w < nw;  // ... of a real walker
-  XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);    // current positions
   XP<R>* PN = reinterpret_cast<XP<R>*>(smem + S.o_pnew);  // proposal
+  // current positions: coordinate q of electron e of local walker wl at
+  // P[wl * pw + (3 e + q) * pq]; a block row in shared memory, or the
+  // [coordinate][walker] array after the determinant work arrays in scratch
+  XP<R>* P;
+  int64_t pw, pq;
+  if (S.pos_global) {
+    P = reinterpret_cast<XP<R>*>(scr + ep_layout(d, 0).bytes_per_slot * ss) + w0;
+    pw = 1;
+    pq = ss;
+  } else {
+    P = reinterpret_cast<XP<R>*>(smem + S.o_pos);
+    pw = ps;
+    pq = 1;
+  }
   double* PSI = reinterpret_cast<double*>(smem + S.o_psi);
   double* F = reinterpret_cast<double*>(smem + S.o_f);
   int* IEL = reinterpret_cast<int*>(smem + S.o_iel);
   int* ACC = reinterpret_cast<int*>(smem + S.o_acc);
   const EPPtrs ptrs{smem, S};
   const double eps = 1e-16;
-  ep_stage_positions<R>(a.pos, w0, nw, nwb, nc, ps, P);
-  ep_eval<R, JC, false>(d, t, ptrs, P, scr, ss, w0, nw);
+  // the first evaluation reads the staged positions from the proposal rows
+  ep_stage_positions<R>(a.pos, w0, nw, nwb, nc, ps, PN);
+  for (int i = tid; i < nwb * nc; i += blockDim.x) {
+    const int wl2 = i / nc, c = i - wl2 * nc;
+    P[wl2 * pw + c * pq] = PN[wl2 * ps + c];
+  }
+  ep_eval<R, JC, false>(d, t, ptrs, PN, scr, ss, w0, nw);
   int nacc = 0;
   double psi_cur = 0.0;  // combine threads: psi at the current positions
   if (tid < nwb) {
@@ -83,7 +101,8 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
         const bool moves = live && (a.move_type == QMC_MOVE_ALL_ELEC ||
                                     (a.move_type == QMC_MOVE_ALL_ELEC_ITER ? e == im : e == IEL[wl]));
         XP<R>* pn = PN + wl * ps + 3 * e;
-        const XP<R>* pc = P + wl * ps + 3 * e;
+        const XP<R> pc[3] = {P[wl * pw + (3 * e) * pq], P[wl * pw + (3 * e + 1) * pq],
+                             P[wl * pw + (3 * e + 2) * pq]};
         if (moves) {
           const double* rp =
               !a.proposals ? nullptr
@@ -122,7 +141,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
       __syncthreads();
       if (live && ACC[wl])
         for (int e = slot; e < ne; e += nslot)
-          for (int q = 0; q < 3; ++q) P[wl * ps + 3 * e + q] = PN[wl * ps + 3 * e + q];
+          for (int q = 0; q < 3; ++q) P[wl * pw + (3 * e + q) * pq] = PN[wl * ps + 3 * e + q];
       __syncthreads();
     }
     if (istep >= a.ntherm) {
@@ -130,7 +149,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
         if (a.samples && isnap < a.nsnap && live)
           for (int e = slot; e < ne; e += nslot) {
             double* out = a.samples + (isnap * nw + w) * nc + 3 * e;
-            for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * ps + 3 * e + q]);
+            for (int q = 0; q < 3; ++q) out[q] = xp_value<R>(P[wl * pw + (3 * e + q) * pq]);
           }
         ++isnap;
       }
@@ -139,7 +158,7 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
   }
   if (live)
     for (int e = slot; e < ne; e += nslot)
-      for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * ps + 3 * e + q]);
+      for (int q = 0; q < 3; ++q) a.pos[w * nc + 3 * e + q] = xp_value<R>(P[wl * pw + (3 * e + q) * pq]);
   if (tid < nwb && w0 + tid < nw) {
     if (a.accepted) a.accepted[w0 + tid] += nacc;
     if (a.psi_out) a.psi_out[w0 + tid] = psi_cur;
@@ -216,6 +235,20 @@ int launch_metropolis_batch(const qmc_wf_desc* descs, const qmc_metropolis_args*
   if (st) return st;
   metropolis_batch_kernel<R, JC><<<(unsigned)b.block0[njobs], nthreads, smem, s>>>(b);
   return launch_status();
+}
+
+// The launch plan launch_metropolis takes for nw walkers: walkers per block,
+// threads per walker, threads per block, positions in scratch (0 / 1),
+// dynamic shared memory bytes.
+template <typename R, int JC>
+int plan_metropolis(const qmc_wf_desc* d, int64_t nw, int32_t* out) {
+  const EPShape S = ep_plan<R>(*d, 2, JC, metropolis_kernel<R, JC>, nw);
+  out[0] = S.nwb;
+  out[1] = S.nslot;
+  out[2] = S.nthreads;
+  out[3] = S.pos_global;
+  out[4] = (int32_t)S.smem;
+  return S.smem < 0 ? QMC_ERR_SHAPE : QMC_OK;
 }
 
 template <typename R, int JC>

@@ -10,6 +10,7 @@ namespace qmc {
 template int launch_metropolis<QMC_INST_R, QMC_INST_JC>(const qmc_wf_desc*,
                                                         const qmc_metropolis_args*,
                                                         unsigned char*, cudaStream_t);
+template int plan_metropolis<QMC_INST_R, QMC_INST_JC>(const qmc_wf_desc*, int64_t, int32_t*);
 template int launch_metropolis_batch<QMC_INST_R, QMC_INST_JC>(const qmc_wf_desc*,
                                                               const qmc_metropolis_args*,
                                                               void* const*, int, cudaStream_t);

@@ -290,10 +290,16 @@ class GPUExecutor:
 
     @staticmethod
     def _launch_key(wf):
-        """Jobs that can share one qmc_metropolis_run_batch launch: the same
-        precision and MO column class of the determinants (any molecule)."""
+        """Jobs grouped into one qmc_metropolis_run_batch launch: the same
+        precision and MO column class of the determinants (what the kernel
+        requires; any molecule otherwise), and electron counts within one band
+        of six. A launch runs with the largest job's block size and shared
+        memory, so the band keeps the jobs' per-step costs and occupancies
+        alike (a small molecule batched with a large one would run at the
+        large one's occupancy)."""
         n = wf.highest_occ_mo
-        return (wf.precision, 0 if n <= 8 else (1 if n <= 16 else 2))
+        return (wf.precision, 0 if n <= 8 else (1 if n <= 16 else 2),
+                (wf.mol.nelec - 1) // 6)
 
     def footprint(self, req):
         mol = self._molecule(req)

@@ -113,3 +113,40 @@ def test_batch_size_does_not_change_results(precision):
                        init=mol.domain("atomic"), cuda=True, seed=9)
         outs.append(s(wf.pdf, pos=x.clone(), with_tqdm=False)[:64].detach().cpu().numpy())
     np.testing.assert_array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_large_chain_plan_does_not_change_results(precision):
+    """H20 sto-3g at 16384 walkers has no one-wave launch plan with the
+    current positions in shared memory; the mixed method's plan keeps them in
+    the scratch instead (one wave). A chain of the first 64 walkers (whose plan keeps them in shared
+    memory) is bitwise the same as inside the 16384-walker batch."""
+    from qmctorch_gb300.sampler import Metropolis
+    from qmctorch_gb300.scf import Molecule
+    from qmctorch_gb300.serving import hydrogen_chain, seeded_positions
+    from qmctorch_gb300.wavefunction import SlaterJastrow
+    torch.set_default_dtype(torch.float64)
+    mol = Molecule(hydrogen_chain(20, 0.95), unit="angs", basis="sto-3g", calculator="huckel")
+    wf = SlaterJastrow(mol, cuda=True, precision=precision)
+    big = torch.as_tensor(seeded_positions(mol, 16384, seed=20), device="cuda")
+    small = big[:64].clone()
+    import ctypes
+
+    from qmctorch_gb300 import _lib
+    call = wf._desc(torch.device("cuda"))
+    plans = {}
+    for nw in (64, 16384):
+        plan = (ctypes.c_int32 * 5)()
+        assert _lib.lib().qmc_metropolis_plan(call.ref, nw, plan) == 0
+        plans[nw] = list(plan)
+    assert plans[64][3] == 0, plans
+    if precision == "mixed":  # one wave: 4 blocks of 32 walkers per SM
+        assert plans[16384][3] == 1 and 152 * 4 * plans[16384][0] >= 16384, plans
+    print("H20 %s plans (nwb, nslot, threads, pos in scratch, smem):" % precision, plans)
+    outs = []
+    for x in (small, big):
+        s = Metropolis(nwalkers=len(x), nstep=12, step_size=0.2, nelec=mol.nelec,
+                       init=mol.domain("atomic"), cuda=True, seed=21)
+        outs.append(s(wf.pdf, pos=x.clone(), with_tqdm=False)[:64].detach().cpu().numpy())
+    np.testing.assert_array_equal(outs[0], outs[1])
+    assert np.isfinite(outs[1]).all()
