@@ -917,6 +917,106 @@ __device__ inline void ep_det(const qmc_wf_desc& d, const EPLayout& L, unsigned 
   spin_channel<R, OP, T>(d, spin, mo, bk, wk, SpinOut<T>{dv, ov, ss, &dref[spin * nwb + wl]});
 }
 
+// Block-cooperative LU of the psi / Metropolis determinant phase for spin
+// channels beyond the register path (excitation mode, in place in the
+// shared-memory MO rows). The nslot threads of a walker split its two
+// channels: slots of even parity serve spin up, odd spin down; the T threads
+// of a channel (rank r = slot / 2) swap the pivot rows by columns j = r mod T
+// and eliminate rows i = k + 1 + r mod T. Every element sees lu_factor's
+// operations in lu_factor's order (the same pivot choice, l = a_ik / a_kk as
+// a_ik * (1 / a_kk), one fma per update), so the factors, pivots and det are
+// bitwise those of the one-thread factorisation. Rank 0 of a channel is the
+// thread the one-thread path runs on (slot = spin, tid < 2 nwb): it keeps the
+// pivots and det, and then solves the virtual columns and forms the
+// excitation values as ep_det does. Three block barriers per elimination step.
+constexpr int kCoopMinN = 6;
+
+template <typename R>
+__host__ __device__ inline bool coop_lu_applies(const qmc_wf_desc& d, int nslot) {
+  if (d.det_mode != QMC_DET_EXCITATION || nslot < 4) return false;
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  if (nmax < kCoopMinN) return false;
+  for (int s = 0; s < 2; ++s) {  // the register path serves both channels
+    const int n = s ? d.ndown : d.nup;
+    const int nv = d.max_orb[s] - n;
+    if (n > kRegMaxN<R> || nv > kRegNV) return true;
+  }
+  return false;
+}
+
+template <typename R, typename T>
+__device__ inline void ep_det_coop(const qmc_wf_desc& d, const EPLayout& L, unsigned char* dbase,
+                                   int64_t dss, int64_t w0, int64_t nw, bool dsm, R* MO, int nwb,
+                                   int nslot, double* DREF) {
+  const int tid = threadIdx.x;
+  const int slot = tid / nwb, wl = tid - slot * nwb;
+  const int spin = slot & 1, r = slot >> 1;
+  const int nt = (nslot - spin + 1) >> 1;  // threads of this channel
+  const bool on = slot < nslot;
+  const int n = spin ? d.ndown : d.nup;
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  const int64_t cs = nwb, rs = (int64_t)d.nmo_used * nwb;
+  R* A = MO + (spin ? d.nup : 0) * rs + wl;
+  int piv[QMC_MAX_NSPIN];
+  double det = 1.0;
+  for (int k = 0; k < nmax; ++k) {
+    const bool act = on && k < n;
+    int p = k;
+    if (act) {
+      R amax = fabs(A[k * rs + k * cs]);
+      for (int i = k + 1; i < n; ++i) {
+        const R v = fabs(A[i * rs + k * cs]);
+        if (v > amax) {
+          amax = v;
+          p = i;
+        }
+      }
+    }
+    __syncthreads();  // column k read by every thread of the channel
+    if (act && p != k)
+      for (int j = r; j < n; j += nt) {
+        const R tmp = A[k * rs + j * cs];
+        A[k * rs + j * cs] = A[p * rs + j * cs];
+        A[p * rs + j * cs] = tmp;
+      }
+    __syncthreads();  // pivot row in place
+    R inv = (R)0;
+    if (act) {
+      const R akk = A[k * rs + k * cs];
+      if (r == 0) {
+        piv[k] = p;
+        if (p != k) det = -det;
+        det *= (double)akk;
+      }
+      inv = akk != (R)0 ? (R)1 / akk : (R)0;
+      for (int i = k + 1 + r; i < n; i += nt) {
+        const R l = A[i * rs + k * cs] * inv;
+        A[i * rs + k * cs] = l;
+        for (int j = k + 1; j < n; ++j) A[i * rs + j * cs] = fma(-l, A[k * rs + j * cs], A[i * rs + j * cs]);
+      }
+    }
+    __syncthreads();  // step k's updates done before the next pivot search
+    // a_kk is read by no later step of the factorisation: stored after the barrier
+    if (act && r == 0) A[k * rs + k * cs] = inv;
+  }
+  if (tid < 2 * nwb && w0 + wl < nw) {
+    using V = T;
+    const int64_t w = dsm ? wl : w0 + wl;
+    V* dv = rptr<V>(dbase, L.dv, dss, w) + (spin ? d.ndet[0] * dss : 0);
+    const int nv = d.max_orb[spin] - n;
+    if (n == 0) {
+      for (int u = 0; u < d.ndet[spin]; ++u) dv[u * dss] = (V)1;
+      DREF[spin * nwb + wl] = 1.0;
+      return;
+    }
+    DREF[spin * nwb + wl] = det;
+    const MView<R> LU{A, rs, cs};
+    const MView<R> X{A + n * cs, rs, cs};
+    if (nv > 0) lu_solve<R>(LU, n, piv, X.c(), X, nv);
+    excitation_values<R, V>(d, d.det_table[spin], spin, X.c(), nv > 0 ? nv : 1, dv, dss);
+  }
+}
+
 struct EPPtrs {
   unsigned char* smem;
   EPShape S;
@@ -952,7 +1052,9 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   const bool dsm = S.o_det >= 0;  // work arrays in shared memory: slot = local walker
   unsigned char* const dbase = dsm ? p.smem + S.o_det : scr;
   const int64_t dss = dsm ? nwb : ss;
-  if (tid < 2 * nwb) {
+  if (!KIN && coop_lu_applies<R>(d, S.nslot)) {
+    ep_det_coop<R, R>(d, L, dbase, dss, w0, nw, dsm, MO, nwb, S.nslot, DREF);
+  } else if (tid < 2 * nwb) {
     const int spin = tid / nwb, wl = tid - spin * nwb;
     if (w0 + wl < nw)
       ep_det<R, KIN>(d, L, dbase, dss, dsm ? wl : w0 + wl, spin, MO, BK, wl, nwb, DREF,
