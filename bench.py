@@ -315,6 +315,15 @@ def bench_h_n(torch, lib, device, flush, nw=16384, nstep=50):
         t = _timed(torch, lambda i: metropolis_capi(torch, lib, wf, x, nstep, 0, STEP_SIZE, 6 + i,
                                                     scratch=scr), 3, flush) / 3
         out["walker_steps_per_s"]["H%d" % n] = nw * nstep / t
+        # stated error of the mixed method: psi against the FP64 method on 4096 of
+        # the sampled positions (FP32 MO values: about kappa * 6e-8 relative)
+        wf64 = SlaterJastrow(mol, cuda=True, precision="fp64")
+        with torch.no_grad():
+            xs = x[:4096].clone()
+            p64 = wf64(xs).reshape(-1)
+            rel = ((wf(xs).reshape(-1) - p64) / p64).abs()
+        out.setdefault("psi_rel_err_vs_fp64_median", {})["H%d" % n] = float(rel.median())
+        out.setdefault("psi_rel_err_vs_fp64_p90", {})["H%d" % n] = float(torch.quantile(rel, 0.9))
     return out
 
 
@@ -530,7 +539,10 @@ def bench_serving(args):
     from qmctorch_gb300.serving import (VMCServer, latency_percentiles, poisson_stream,
                                         replay_stream)
     out = {"workload": "h_n_sto3g_single_point_stream", "requests_per_rate": args.serve_requests,
-           "hbm_budget_bytes": args.serve_budget_gb << 30, "slice_steps": 256, "rates": []}
+           "hbm_budget_bytes": args.serve_budget_gb << 30, "slice_steps": 256,
+           "precision": "auto: the mixed method where its median psi error against FP64 "
+                        "(256 seeded positions per molecule) is <= 1e-4, else FP64",
+           "rates": []}
     # warm-up: build and load every shape once (kernels, plans, molecules)
     warm = VMCServer(hbm_budget=args.serve_budget_gb << 30)
     replay_stream(warm, poisson_stream(8, 1000.0, seed=99, smin=20, smax=20, wmin=256,
@@ -545,7 +557,8 @@ def bench_serving(args):
                              "p50_latency_s": lat["p50"], "p99_latency_s": lat["p99"],
                              "walker_steps_per_s": ws / makespan, "makespan_s": makespan,
                              "launches": srv.launches,
-                             "jobs_per_launch": srv.launched_jobs / max(srv.launches, 1)})
+                             "jobs_per_launch": srv.launched_jobs / max(srv.launches, 1),
+                             "fp64_requests": sum(r.precision == "fp64" for r in res)})
     return out
 
 
@@ -586,6 +599,9 @@ def summarize(line, results, args, units, world, m_met, m_el, f_met, f_el):
         ws = h["walker_steps_per_s"]
         out["h_n_walker_steps_per_s"] = {k: _r(ws[k], 3) for k in ("H8", "H16", "H20", "H32")
                                          if k in ws}
+        er = h.get("psi_rel_err_vs_fp64_median", {})
+        out["h_n_mixed_psi_rel_err_median"] = {k: _r(er[k], 2) for k in ("H8", "H12", "H16", "H20")
+                                               if k in er}
     mt = line.get("mo_tensor_core")
     if mt and "c6h6_ccpvdz" in mt:
         out["mo_tc_c6h6"] = {"ms": _r(mt["c6h6_ccpvdz"]["ms_tc"], 3),

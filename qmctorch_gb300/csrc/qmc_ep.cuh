@@ -944,20 +944,16 @@ __host__ __device__ inline bool coop_lu_applies(const qmc_wf_desc& d, int nslot)
   return false;
 }
 
-template <typename R, typename T>
-__device__ inline void ep_det_coop(const qmc_wf_desc& d, const EPLayout& L, unsigned char* dbase,
-                                   int64_t dss, int64_t w0, int64_t nw, bool dsm, R* MO, int nwb,
-                                   int nslot, double* DREF) {
-  const int tid = threadIdx.x;
-  const int slot = tid / nwb, wl = tid - slot * nwb;
-  const int spin = slot & 1, r = slot >> 1;
-  const int nt = (nslot - spin + 1) >> 1;  // threads of this channel
-  const bool on = slot < nslot;
-  const int n = spin ? d.ndown : d.nup;
-  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
-  const int64_t cs = nwb, rs = (int64_t)d.nmo_used * nwb;
-  R* A = MO + (spin ? d.nup : 0) * rs + wl;
-  int piv[QMC_MAX_NSPIN];
+// The elimination steps of the block-cooperative LU of this thread's channel
+// matrix A(i, j) = A[i rs + j cs] (n x n; on: the thread serves a channel of
+// rank r among nt threads). Every thread of the block calls it: three block
+// barriers per step up to nmax, and one at the end, after which the factors
+// (unit lower, upper with inverted diagonal, as lu_factor leaves them), the
+// pivots piv[0..n) and det (the return value) are valid on every thread of the
+// channel.
+template <typename R>
+__device__ inline double coop_lu_steps(R* A, int64_t rs, int64_t cs, int n, int nmax, bool on,
+                                       int r, int nt, int* piv) {
   double det = 1.0;
   for (int k = 0; k < nmax; ++k) {
     const bool act = on && k < n;
@@ -983,11 +979,9 @@ __device__ inline void ep_det_coop(const qmc_wf_desc& d, const EPLayout& L, unsi
     R inv = (R)0;
     if (act) {
       const R akk = A[k * rs + k * cs];
-      if (r == 0) {
-        piv[k] = p;
-        if (p != k) det = -det;
-        det *= (double)akk;
-      }
+      piv[k] = p;
+      if (p != k) det = -det;
+      det *= (double)akk;
       inv = akk != (R)0 ? (R)1 / akk : (R)0;
       for (int i = k + 1 + r; i < n; i += nt) {
         const R l = A[i * rs + k * cs] * inv;
@@ -995,11 +989,52 @@ __device__ inline void ep_det_coop(const qmc_wf_desc& d, const EPLayout& L, unsi
         for (int j = k + 1; j < n; ++j) A[i * rs + j * cs] = fma(-l, A[k * rs + j * cs], A[i * rs + j * cs]);
       }
     }
-    __syncthreads();  // step k's updates done before the next pivot search
+    __syncthreads();  // step k's updates and a_kk reads done
     // a_kk is read by no later step of the factorisation: stored after the barrier
     if (act && r == 0) A[k * rs + k * cs] = inv;
   }
-  if (tid < 2 * nwb && w0 + wl < nw) {
+  __syncthreads();  // the inverted diagonal in place for the solves
+  return det;
+}
+
+// Thread roles of the cooperative determinant phase: the walker's even slots
+// serve spin up, the odd ones spin down; rank r = slot / 2.
+struct CoopRole {
+  int slot, wl, spin, r, nt;
+  bool on;
+  __device__ CoopRole(int nwb, int nslot) {
+    const int tid = threadIdx.x;
+    slot = tid / nwb;
+    wl = tid - slot * nwb;
+    spin = slot & 1;
+    r = slot >> 1;
+    nt = (nslot - spin + 1) >> 1;
+    on = slot < nslot;
+  }
+};
+
+// The local-energy kernel's cooperative path: the channels beyond the
+// register path of the mixed local energy (el_regs), from six electrons.
+template <typename R>
+__host__ __device__ inline bool coop_el_applies(const qmc_wf_desc& d, int nslot) {
+  if (d.det_mode != QMC_DET_EXCITATION || nslot < 4 || el_regs(d)) return false;
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  return nmax >= kCoopMinN;
+}
+
+template <typename R, typename T>
+__device__ inline void ep_det_coop(const qmc_wf_desc& d, const EPLayout& L, unsigned char* dbase,
+                                   int64_t dss, int64_t w0, int64_t nw, bool dsm, R* MO, int nwb,
+                                   int nslot, double* DREF) {
+  const CoopRole c(nwb, nslot);
+  const int spin = c.spin, wl = c.wl;
+  const int n = spin ? d.ndown : d.nup;
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  const int64_t cs = nwb, rs = (int64_t)d.nmo_used * nwb;
+  R* A = MO + (spin ? d.nup : 0) * rs + wl;
+  int piv[QMC_MAX_NSPIN];
+  const double det = coop_lu_steps<R>(A, rs, cs, n, nmax, c.on, c.r, c.nt, piv);
+  if (threadIdx.x < 2 * nwb && w0 + wl < nw) {
     using V = T;
     const int64_t w = dsm ? wl : w0 + wl;
     V* dv = rptr<V>(dbase, L.dv, dss, w) + (spin ? d.ndet[0] * dss : 0);
@@ -1017,6 +1052,78 @@ __device__ inline void ep_det_coop(const qmc_wf_desc& d, const EPLayout& L, unsi
   }
 }
 
+// Local-energy determinant phase of large excitation-mode channels with the
+// walker's threads: the channel's T threads copy the occupied block to the LU
+// work array by rows, factor it cooperatively (coop_lu_steps), and solve the
+// right-hand sides by columns (A^-1 A_virt and A^-1 [B_occ | B_virt], each
+// column with its FP64 residual refinement in the mixed method: the column
+// solves are independent, so the values are spin_channel's bitwise); the
+// channel's first thread then forms the determinant ratios and traces
+// (excitation_tail). Two more block barriers.
+template <typename R>
+__device__ inline void ep_det_el_coop(const qmc_wf_desc& d, const EPLayout& L,
+                                      unsigned char* dbase, int64_t dss, int64_t w0, int64_t nw,
+                                      bool dsm, R* MO, R* BK, int nwb, int nslot, double* DREF) {
+  constexpr bool REFINE = kMixed<R>;
+  const CoopRole c(nwb, nslot);
+  const int spin = c.spin, wl = c.wl, r = c.r, nt = c.nt;
+  const int n = spin ? d.ndown : d.nup;
+  const int nv = d.max_orb[spin] - n;
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  const int64_t cs = nwb, rs = (int64_t)d.nmo_used * nwb;
+  const int row0 = spin ? d.nup : 0;
+  const CView<R> mo{MO + row0 * rs + wl, rs, cs};
+  const CView<R> bk{BK + row0 * rs + wl, rs, cs};
+  const CView<R> avirt{mo.p + n * cs, rs, cs};
+  const int64_t w = dsm ? wl : w0 + wl;
+  const int64_t vm = L.vmax > 0 ? L.vmax : 1;
+  SpinWork<R> wk;
+  wk.LU = MView<R>{rptr<R>(dbase, L.lu[spin], dss, w), (int64_t)L.nmax * dss, dss};
+  wk.X = MView<R>{rptr<R>(dbase, L.x[spin], dss, w), vm * dss, dss};
+  wk.Y = MView<R>{rptr<R>(dbase, L.y[spin], dss, w), (int64_t)L.omax * dss, dss};
+  wk.rc = MView<R>{rptr<R>(dbase, L.rc[spin], dss, w), dss, dss};
+  wk.X64 = MView<double>{rptr<double>(dbase, L.x64[spin], dss, w), vm * dss, dss};
+  wk.Y64 = MView<double>{rptr<double>(dbase, L.y64[spin], dss, w), (int64_t)L.omax * dss, dss};
+  if (c.on)
+    for (int i = r; i < n; i += nt)
+      for (int j = 0; j < n; ++j) wk.LU(i, j) = mo(i, j);
+  __syncthreads();  // the occupied block copied
+  int piv[QMC_MAX_NSPIN];
+  const double det = coop_lu_steps<R>(wk.LU.p, wk.LU.rs, wk.LU.cs, n, nmax, c.on, r, nt, piv);
+  if (c.on && n > 0) {
+    // this thread's columns; a private residual column for the refinements
+    R rcl[QMC_MAX_NSPIN];
+    const MView<R> rc{rcl, 1, 1};
+    auto col = [](MView<R> m, int j) { return MView<R>{m.p + j * m.cs, m.rs, m.cs}; };
+    auto ccol = [](CView<R> m, int j) { return CView<R>{m.p + j * m.cs, m.rs, m.cs}; };
+    for (int j = r; j < nv; j += nt) lu_solve<R>(wk.LU, n, piv, ccol(avirt, j), col(wk.X, j), 1);
+    for (int j = r; j < n + nv; j += nt) lu_solve<R>(wk.LU, n, piv, ccol(bk, j), col(wk.Y, j), 1);
+    if (REFINE) {
+      for (int j = r; j < nv; j += nt)
+        lu_refine<R>(wk.LU, n, piv, mo, ccol(avirt, j), col(wk.X, j),
+                     MView<double>{wk.X64.p + j * wk.X64.cs, wk.X64.rs, wk.X64.cs}, rc, 1);
+      for (int j = r; j < n + nv; j += nt)
+        lu_refine<R>(wk.LU, n, piv, mo, ccol(bk, j), col(wk.Y, j),
+                     MView<double>{wk.Y64.p + j * wk.Y64.cs, wk.Y64.rs, wk.Y64.cs}, rc, 1);
+    }
+  }
+  __syncthreads();  // every column solved
+  if (threadIdx.x < 2 * nwb && w0 + wl < nw) {
+    double* dv = rptr<double>(dbase, L.dv, dss, w) + (spin ? d.ndet[0] * dss : 0);
+    double* ov = rptr<double>(dbase, L.ov, dss, w) + (spin ? d.ndet[0] * dss : 0);
+    if (n == 0) {
+      for (int u = 0; u < d.ndet[spin]; ++u) {
+        dv[u * dss] = 1.0;
+        ov[u * dss] = 0.0;
+      }
+      DREF[spin * nwb + wl] = 1.0;
+      return;
+    }
+    DREF[spin * nwb + wl] = det;
+    excitation_tail<R, true, double>(d, spin, n, nv, wk, SpinOut<double>{dv, ov, dss, &DREF[spin * nwb + wl]});
+  }
+}
+
 struct EPPtrs {
   unsigned char* smem;
   EPShape S;
@@ -1026,7 +1133,10 @@ struct EPPtrs {
 // block's walkers at split positions `pbuf` (shared memory, [nwb][3 nelec]).
 // Results in shared memory: psi[wl], and with KIN kin[wl], v[wl] (V_en + V_ee).
 // Every thread of the block must call this (it contains block barriers).
-template <typename R, int JC, bool KIN>
+// ELCOOP: the local-energy kernel instance with the cooperative determinant
+// phase of large channels (a separate instance: its work arrays and pivots
+// would cost the small-molecule local-energy kernel registers).
+template <typename R, int JC, bool KIN, bool ELCOOP = false>
 __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const EPPtrs& p,
                                const XP<R>* pbuf, unsigned char* scr, int64_t ss, int64_t w0,
                                int64_t nw) {
@@ -1054,6 +1164,8 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   const int64_t dss = dsm ? nwb : ss;
   if (!KIN && coop_lu_applies<R>(d, S.nslot)) {
     ep_det_coop<R, R>(d, L, dbase, dss, w0, nw, dsm, MO, nwb, S.nslot, DREF);
+  } else if (KIN && ELCOOP && coop_el_applies<R>(d, S.nslot)) {
+    if constexpr (KIN && ELCOOP) ep_det_el_coop<R>(d, L, dbase, dss, w0, nw, dsm, MO, BK, nwb, S.nslot, DREF);
   } else if (tid < 2 * nwb) {
     const int spin = tid / nwb, wl = tid - spin * nwb;
     if (w0 + wl < nw)

@@ -63,8 +63,14 @@ struct Shape {
   int kc;        // stored depth 2 kp ([hi | lo])
   int n;         // MMA N (nmo rounded up to 16)
   int acc_cols;  // TMEM columns of one accumulator: power of two >= max(32, n)
-  int64_t a_off[2], b_off, bar_off, smem;
+  int64_t a_off[2], b_off, st_off, bar_off, smem;
 };
+
+// Epilogue staging: per epilogue warp a 32-row x 16-column FP32 block, rows
+// kStageStride floats apart (20: the 16-byte row stores of a quarter warp fall
+// on distinct banks).
+constexpr int kStageStride = 20;
+constexpr int kStageBytes = 32 * kStageStride * 4;
 
 // barriers at bar_off: full[2], empty[2], dfull[2], dempty[2] (8 B each), then
 // the TMEM address (4 B) and the abort flag (4 B)
@@ -81,7 +87,8 @@ __host__ __device__ inline Shape shape(int nao, int nmo) {
   s.a_off[0] = 0;
   s.a_off[1] = a_bytes;
   s.b_off = 2 * a_bytes;
-  s.bar_off = s.b_off + (int64_t)s.n * s.kc * 2;
+  s.st_off = s.b_off + (int64_t)s.n * s.kc * 2;
+  s.bar_off = s.st_off + (int64_t)kEpilogueWarps * kStageBytes;
   s.smem = s.bar_off + kNumBars * 8 + 8 + 1024;  // 1 KB for base alignment
   return s;
 }
@@ -371,24 +378,39 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
       if (!ok) break;
       fence_after_sync();
       const uint32_t dt = tmem + (uint32_t)(d * S.acc_cols) + ((uint32_t)(q * 32) << 16);
-      const int64_t row = tile * kM + q * 32 + lane;
+      const int64_t row0 = tile * kM + q * 32;  // this warp's 32 rows
+      // transpose through shared memory: lane l holds row l's 16 columns after
+      // tcgen05.ld; after the exchange, lane l writes columns 2 (l % 8), + 1 of
+      // row 4 j + l / 8, so each store instruction covers four rows' 128
+      // contiguous bytes instead of 16 bytes of 32 rows
+      float* stg = reinterpret_cast<float*>(smem + S.st_off) +
+                   (warp - kMmaWarp - 1) * (kStageBytes / 4);
+      const int rsub = lane >> 3, csub = 2 * (lane & 7);
       for (int ch = half; ch < nchunk; ch += 2) {
         float v[16];
         tmem_ld16(dt + (uint32_t)(ch * 16), v);
-        if (row < nrows) {
-          double* dst = mo + row * nmo + ch * 16;
-          if (vec) {
 #pragma unroll
-            for (int j = 0; j < 8; ++j)
-              if (ch * 16 + 2 * j < nmo)
-                reinterpret_cast<double2*>(dst)[j] = make_double2((double)v[2 * j],
-                                                                  (double)v[2 * j + 1]);
-          } else {
+        for (int j = 0; j < 4; ++j)
+          *reinterpret_cast<float4*>(stg + lane * kStageStride + 4 * j) =
+              make_float4(v[4 * j], v[4 * j + 1], v[4 * j + 2], v[4 * j + 3]);
+        __syncwarp();
+        const int col = ch * 16 + csub;
 #pragma unroll
-            for (int j = 0; j < 16; ++j)
-              if (ch * 16 + j < nmo) dst[j] = (double)v[j];
+        for (int j = 0; j < 8; ++j) {
+          const int r = 4 * j + rsub;
+          const int64_t row = row0 + r;
+          const float2 f = *reinterpret_cast<const float2*>(stg + r * kStageStride + csub);
+          if (row < nrows && col < nmo) {
+            double* dst = mo + row * nmo + col;
+            if (vec) {  // nmo even: col + 1 < nmo and 16-byte alignment
+              *reinterpret_cast<double2*>(dst) = make_double2((double)f.x, (double)f.y);
+            } else {
+              dst[0] = (double)f.x;
+              if (col + 1 < nmo) dst[1] = (double)f.y;
+            }
           }
         }
+        __syncwarp();
       }
       fence_before_sync();
       mbar_arrive(bars + 8 * (kBarDEmpty + d));

@@ -28,7 +28,7 @@ __global__ void __launch_bounds__(EPBound<R>::kThreads) ep_psi_kernel(const qmc_
     psi[w0 + tid] = reinterpret_cast<const double*>(smem + S.o_psi)[tid];
 }
 
-template <typename R, int JC>
+template <typename R, int JC, bool ELCOOP = false>
 __global__ void __launch_bounds__(EPElBound<R>::kThreads) ep_eloc_kernel(const qmc_wf_desc d, const double* __restrict__ pos,
                                                        int64_t nw, double* __restrict__ eloc,
                                                        double* __restrict__ kin,
@@ -40,7 +40,7 @@ __global__ void __launch_bounds__(EPElBound<R>::kThreads) ep_eloc_kernel(const q
   const int64_t w0 = (int64_t)blockIdx.x * S.nwb;
   XP<R>* P = reinterpret_cast<XP<R>*>(smem + S.o_pos);
   ep_stage_positions<R>(pos, w0, nw, S.nwb, 3 * d.nelec, S.pstride, P);
-  ep_eval<R, JC, true>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
+  ep_eval<R, JC, true, ELCOOP>(d, t, EPPtrs{smem, S}, P, scr, ss, w0, nw);
   const int tid = threadIdx.x;
   if (tid < S.nwb && w0 + tid < nw) {
     const double k = reinterpret_cast<const double*>(smem + S.o_kin)[tid];
@@ -77,16 +77,26 @@ static int dispatch_psi(const qmc_wf_desc* d, const double* pos, int64_t nw, dou
   return launch_psi<R, 24>(d, pos, nw, psi, scr, s);
 }
 
+template <typename R, int JC, bool ELCOOP>
+static int launch_eloc_k(const qmc_wf_desc* d, const double* pos, int64_t nw, double* eloc,
+                         double* kin, double* psi, unsigned char* scr, cudaStream_t s) {
+  const EPShape S = ep_plan<R>(*d, 1, JC, ep_eloc_kernel<R, JC, ELCOOP>, nw);
+  int st = launch_prepare<R>(ep_eloc_kernel<R, JC, ELCOOP>, S, 1);
+  if (st) return st;
+  const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
+  ep_eloc_kernel<R, JC, ELCOOP><<<grid, S.nthreads, S.smem, s>>>(*d, pos, nw, eloc, kin, psi,
+                                                                 scr, pad_walkers(nw), S);
+  return launch_status();
+}
+
+// Molecules with large excitation-mode channels (beyond the register path)
+// run the instance with the cooperative determinant phase.
 template <typename R, int JC>
 static int launch_eloc(const qmc_wf_desc* d, const double* pos, int64_t nw, double* eloc,
                        double* kin, double* psi, unsigned char* scr, cudaStream_t s) {
-  const EPShape S = ep_plan<R>(*d, 1, JC, ep_eloc_kernel<R, JC>, nw);
-  int st = launch_prepare<R>(ep_eloc_kernel<R, JC>, S, 1);
-  if (st) return st;
-  const dim3 grid((unsigned)((nw + S.nwb - 1) / S.nwb));
-  ep_eloc_kernel<R, JC><<<grid, S.nthreads, S.smem, s>>>(*d, pos, nw, eloc, kin, psi, scr,
-                                                         pad_walkers(nw), S);
-  return launch_status();
+  if (coop_el_applies<R>(*d, 4))
+    return launch_eloc_k<R, JC, true>(d, pos, nw, eloc, kin, psi, scr, s);
+  return launch_eloc_k<R, JC, false>(d, pos, nw, eloc, kin, psi, scr, s);
 }
 
 }  // namespace qmc

@@ -52,6 +52,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 MAX_BATCH = 32  # QMC_MAX_BATCH of qmc_metropolis_run_batch
+AUTO_PSI_TOL = 1e-4  # "auto" precision: largest median relative psi error of the mixed method
 
 
 @dataclass
@@ -71,7 +72,7 @@ class Request:
     configs: str = "ground_state"
     step_size: float = 0.2
     seed: int = 0
-    precision: str = "mixed"
+    precision: str = "auto"      # "mixed", "fp64", or "auto" (GPUExecutor.precision_of)
     kind: str = "single_point"   # or "run"
     nepoch: int = 0              # run: optimisation epochs
     lr: float = 1e-3             # run: Adam learning rate
@@ -92,6 +93,8 @@ class Result:
     admitted: float
     done: float
     energies: list = None  # run: mean local energy of each epoch
+    precision: str = None  # the method that ran
+    mixed_psi_err: float = None  # "auto": median relative psi error of the mixed method
 
     @property
     def latency(self):
@@ -182,9 +185,12 @@ class Scheduler:
             if job.inflight is not None and self.ex.ready(job.inflight):
                 job.inflight = None
                 if job.phase == "energy":
-                    e, v, err, energies = self.ex.stats(job.handle)
+                    st = self.ex.stats(job.handle)
+                    e, v, err, energies = st[:4]
                     r = Result(job.req.rid, e, v, err, job.req.nwalkers, job.req.nstep,
                                job.req.arrival, job.admitted, self.clock(), energies)
+                    if len(st) > 4:  # the method that ran and, for "auto", its probe
+                        r.precision, r.mixed_psi_err = st[4]
                     self.results[r.rid] = r
                     out.append(r)
                     self.ex.release(job.handle)
@@ -268,6 +274,8 @@ class GPUExecutor:
         self.streams = [torch.cuda.Stream(device=self.device) for _ in range(nstreams)]
         self._mols = {}
         self._sizes = {}
+        self._auto = {}
+        self._probe_stream = torch.cuda.Stream(device=self.device)
 
     def _molecule(self, req):
         from .scf import Molecule
@@ -279,14 +287,42 @@ class GPUExecutor:
                 self._mols.clear()
         return self._mols[k]
 
+    def precision_of(self, req, mol):
+        """(method, probe error) of a request. "auto" takes the mixed method when
+        its psi agrees with the FP64 method within AUTO_PSI_TOL relative (median
+        over 256 seeded positions of the molecule, probed once per molecule),
+        else FP64: the mixed method's FP32 MO values cost about kappa * 6e-8
+        relative in each determinant, kappa the Slater matrix's condition
+        number, which grows about tenfold per H2 unit of a linear chain."""
+        if req.precision != "auto":
+            return req.precision, None
+        k = (req.atoms, req.unit, req.basis, req.calculator, req.configs)
+        if k not in self._auto:
+            from .wavefunction import SlaterJastrow
+            torch = self.torch
+            torch.set_default_dtype(torch.float64)
+            self._probe_stream.wait_stream(torch.cuda.current_stream(self.device))
+            with torch.cuda.stream(self._probe_stream), torch.no_grad():
+                x = torch.as_tensor(seeded_positions(mol, 256, seed=12345), device=self.device)
+                p64 = SlaterJastrow(mol, configs=req.configs, cuda=True,
+                                    precision="fp64")(x).reshape(-1)
+                pm = SlaterJastrow(mol, configs=req.configs, cuda=True,
+                                   precision="mixed")(x).reshape(-1)
+                err = float(((pm - p64) / p64).abs().median())
+            self._auto[k] = ("mixed" if err <= AUTO_PSI_TOL else "fp64", err)
+            if len(self._auto) > 4096:
+                self._auto.clear()
+        return self._auto[k]
+
     def _wf(self, req, mol):
         from .wavefunction import SlaterJastrow
         self.torch.set_default_dtype(self.torch.float64)
-        return SlaterJastrow(mol, configs=req.configs, cuda=True, precision=req.precision)
+        return SlaterJastrow(mol, configs=req.configs, cuda=True,
+                             precision=self.precision_of(req, mol)[0])
 
     def _shape_key(self, req, mol):
         return (mol.nelec, mol.nup, mol.basis.nao, len(mol.atoms), req.basis, req.configs,
-                req.precision)
+                self.precision_of(req, mol)[0])
 
     @staticmethod
     def _launch_key(wf):
@@ -435,7 +471,7 @@ class GPUExecutor:
         energies = None
         if h["req"].kind == "run":
             energies = [float(v) for v in h["host_energies"].tolist()][: h["req"].nepoch]
-        return e, v, err, energies
+        return e, v, err, energies, self.precision_of(h["req"], h["wf"].mol)
 
     def release(self, h):
         h.clear()
@@ -459,7 +495,7 @@ def single_point(req, device=None):
 
 
 def poisson_stream(nreq, rate, seed=0, nmin=2, nmax=32, wmin=1024, wmax=16384, smin=100,
-                   smax=1000, precision="mixed"):
+                   smax=1000, precision="auto"):
     """Seeded request stream: linear H_n chains (n even in [nmin, nmax],
     spacing uniform in 0.7-1.2 angstrom, sto-3g), walkers log-uniform in
     [wmin, wmax], steps uniform in [smin, smax], Poisson arrival times of the

@@ -201,3 +201,19 @@ def test_run_request_lowers_the_energy():
     res = single_point(r)
     e = np.asarray(res.energies)
     assert np.all(np.isfinite(e)) and e[-5:].mean() < e[:5].mean()
+
+
+def test_auto_precision_follows_the_probe():
+    """precision="auto" (the default) runs the mixed method where its psi
+    agrees with FP64 within 1e-4 (median over 256 seeded positions) and FP64
+    elsewhere: a short chain samples in mixed precision, a long one (Slater
+    matrices with condition numbers ~1e10) in FP64; each result records the
+    method and the probe's error."""
+    from qmctorch_gb300.serving import AUTO_PSI_TOL, Request, VMCServer, hydrogen_chain
+    srv = VMCServer(nstreams=2)
+    srv.submit(Request(atoms=hydrogen_chain(4, 0.95), nwalkers=512, nstep=20, seed=1))
+    srv.submit(Request(atoms=hydrogen_chain(24, 0.95), nwalkers=512, nstep=20, seed=2))
+    res = sorted(srv.run(), key=lambda r: r.rid)
+    assert [r.precision for r in res] == ["mixed", "fp64"]
+    assert res[0].mixed_psi_err <= AUTO_PSI_TOL < res[1].mixed_psi_err
+    assert all(np.isfinite(r.energy) for r in res)
