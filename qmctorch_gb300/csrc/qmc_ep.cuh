@@ -188,8 +188,9 @@ __host__ __device__ constexpr int ep_thread_bound(int kind) {
 // AO groups
 // ---------------------------------------------------------------------------
 // Radial sums G_n = sum_p w_cp alpha_p^n exp(-alpha_p r^2) of NC components.
-// CUT: skip primitives with alpha r^2 > kRadialCut (exp < 1e-20), for the
-// single-electron ratio kernel only; every other kernel evaluates all terms.
+// CUT: skip primitives with alpha r^2 > kRadialCut (exp < 1e-20): the FP64
+// electron-parallel kernels and the FP64 single-electron ratio; the mixed
+// method evaluates every term (its FP32 exp is cheap and flushes far below).
 constexpr float kRadialCut = 46.0f;
 
 template <typename R, bool DERIV, int NC, bool CUT = false>
@@ -413,10 +414,13 @@ __device__ __forceinline__ void for_each_ao_ep(const Tables<R>& t, XP<R> ex, XP<
       r2 = dx * dx + dy * dy + dz * dz;
       last = A;
     }
+    // FP64: primitives with alpha r^2 > 46 (exp < 1e-20) are skipped, as a
+    // zero contribution (the FP64 exp is the plain method's costliest
+    // operation; long chains skip most of the far atoms' primitives)
     if (sto)
       group_sto<R, DERIV>(t, g, dx, dy, dz, r2, f);
     else
-      ao_group<R, DERIV>(t, g, dx, dy, dz, r2, f);
+      ao_group<R, DERIV, F, !kMixed<R>>(t, g, dx, dy, dz, r2, f);
   }
 }
 
