@@ -514,13 +514,33 @@ def bench_mo_tensor_core(torch, device, flush, nw_c6h6=16384, nw_h2o=16384):
             W = (wf64.mo.mo_scf * wf64.mo.mo_modifier).to(torch.float64)
             scale = (ao.abs().reshape(rows, nao) @ W.abs()).reshape(ref.shape)
             err = float(((got - ref).abs() / (scale + 1e-300)).max())
-            t_tc = _timed(torch, lambda i: wfm.mo(ao), 5, flush) / 5
-            t_64 = _timed(torch, lambda i: wf64.mo(ao), 3, flush) / 3
+            # the kernels through the C ABI (descriptor built, output allocated
+            # once), and the module call wf.mo(ao) (with its status check)
+            import ctypes
+
+            from qmctorch_gb300 import _lib
+            from qmctorch_gb300.wavefunction import runtime as rt
+            lib = _lib.lib()
+            xa = ao.reshape(-1, nao).contiguous()
+            dst = torch.empty((rows, nmo), dtype=torch.float64, device=device)
+
+            def capi(wf, fn):
+                call = rt.build_desc(device, wf.ao, mo=wf.mo)
+                f = getattr(lib, fn)
+                sh = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+                return lambda i: f(call.ref, ctypes.c_void_p(xa.data_ptr()), rows,
+                                   ctypes.c_void_p(dst.data_ptr()), sh)
+
+            t_tc = _timed(torch, capi(wfm, "qmc_mo_eval_tc"), 5, flush) / 5
+            _lib.check(lib.qmc_mo_eval_tc_status(None), "qmc_mo_eval_tc")
+            t_64 = _timed(torch, capi(wf64, "qmc_mo_eval"), 3, flush) / 3
+            t_mod = _timed(torch, lambda i: wfm.mo(ao), 5, flush) / 5
         nbytes = rows * (nao + nmo) * 8
         kp, npad = (nao + 15) // 16 * 16, (nmo + 15) // 16 * 16
         tc_flops = 2.0 * ((rows + 127) // 128 * 128) * npad * 3 * kp
         out[tag] = {"rows": rows, "nao": nao, "nmo": nmo, "ms_tc": t_tc * 1e3,
                     "ms_fp64": t_64 * 1e3, "speedup_vs_fp64": t_64 / t_tc,
+                    "ms_tc_module_call": t_mod * 1e3,
                     "algorithmic_bytes": nbytes, "achieved_gbs": nbytes / t_tc / 1e9,
                     "frac_of_hbm": nbytes / t_tc / 1e9 / peaks["hbm_gbs"],
                     "tensor_tflops": tc_flops / t_tc / 1e12,

@@ -1156,10 +1156,18 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
   double* KINV = reinterpret_cast<double*>(p.smem + S.o_kin);
   double* V = reinterpret_cast<double*>(p.smem + S.o_v);
   {
+    // electrons dealt to the walker's slots in snake order (slot s takes s,
+    // 2 nslot - 1 - s, 2 nslot + s, ...): psi's Jastrow row of electron e has
+    // ne - 1 - e pairs, and the snake evens the slots' pair counts; each
+    // electron's arithmetic does not depend on the thread that runs it
     const int slot = tid / nwb, wl = tid - (tid / nwb) * nwb;
-    for (int e = slot; e < ne && slot < S.nslot; e += S.nslot)
-      ep_electron<R, JC, KIN>(d, t, pbuf + wl * S.pstride, e, MO + wl, BK + wl, nwb, &JR[e * nwb + wl],
-                              &VR[e * nwb + wl]);
+    const int ns = S.nslot;
+    for (int b = 0; b < ne && slot < ns; b += ns) {
+      const int e = ((b / ns) & 1) ? b + ns - 1 - slot : b + slot;
+      if (e < ne)
+        ep_electron<R, JC, KIN>(d, t, pbuf + wl * S.pstride, e, MO + wl, BK + wl, nwb,
+                                &JR[e * nwb + wl], &VR[e * nwb + wl]);
+    }
   }
   __syncthreads();
   const EPLayout L = ep_layout(d, KIN ? 1 : 0);

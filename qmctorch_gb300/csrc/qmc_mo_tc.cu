@@ -53,6 +53,7 @@ constexpr int kThreads = kWarps * 32;   // 544
 constexpr int kProducerThreads = kProducerWarps * 32;
 constexpr int kEpilogueThreads = kEpilogueWarps * 32;
 constexpr int kMaxN = 256;              // MMA N limit for M = 128
+constexpr int kLoadItems = 3;           // producer items (8 FP64 each) in flight per thread
 constexpr uint64_t kWaitNs = 1000000000ull;  // default pipeline wait limit: 1 s
 
 // Set by a CTA whose pipeline wait ran out (one word per device).
@@ -162,14 +163,46 @@ __device__ inline uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
+// FP64 -> FP32 by integer operations on the bit pattern, truncating the
+// mantissa (relative error below 2^-23; the split keeps 16 bits): exponent
+// rebiased, values below FP32's normal range to a signed zero, above it to
+// infinity. No instruction on the FP64 pipe, which a conversion instruction
+// would occupy at the FP64 rate.
+__device__ __forceinline__ float f32_trunc(double x) {
+  const int hi = __double2hiint(x);
+  const unsigned lo = (unsigned)__double2loint(x);
+  const int e = ((hi >> 20) & 0x7FF) - 896;  // 1023 - 127
+  const unsigned m = ((unsigned)(hi & 0xFFFFF) << 3) | (lo >> 29);
+  const unsigned s = (unsigned)hi & 0x80000000u;
+  const unsigned bits = e <= 0 ? s : (e >= 255 ? (s | 0x7F800000u) : (s | ((unsigned)e << 23) | m));
+  return __uint_as_float(bits);
+}
+
+// FP32 -> FP64 by integer operations on the bit pattern, without branches
+// (the conversion instruction issues on the FP64 pipe): exact for normal
+// values, infinity and NaN; zero and subnormal values (below 1.2e-38) give a
+// signed zero.
+__device__ __forceinline__ double f64_from_f32(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xFFu;
+  const unsigned s = b & 0x80000000u;
+  const unsigned ee = e == 255u ? 2047u : e + 896u;
+  const unsigned hi = e == 0u ? s : (s | (ee << 20) | ((b & 0x7FFFFFu) >> 3));
+  const unsigned lo = e == 0u ? 0u : (b << 29);
+  return __hiloint2double((int)hi, (int)lo);
+}
+
 // Split 8 FP64 values into their BF16 hi and lo parts, packed as 16 bytes each.
+// The split runs in FP32 (x truncated to FP32 first: its 24 bits hold the 16
+// that hi + lo keep, and x_f - hi is exact in FP32), with no FP64 arithmetic.
 __device__ inline void split8(const double (&v)[8], uint4& hi, uint4& lo) {
   uint32_t h[4], l[4];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    const __nv_bfloat16 h0 = __double2bfloat16(v[2 * j]), h1 = __double2bfloat16(v[2 * j + 1]);
-    const __nv_bfloat16 l0 = __double2bfloat16(v[2 * j] - (double)__bfloat162float(h0));
-    const __nv_bfloat16 l1 = __double2bfloat16(v[2 * j + 1] - (double)__bfloat162float(h1));
+    const float f0 = f32_trunc(v[2 * j]), f1 = f32_trunc(v[2 * j + 1]);
+    const __nv_bfloat16 h0 = __float2bfloat16(f0), h1 = __float2bfloat16(f1);
+    const __nv_bfloat16 l0 = __float2bfloat16(f0 - __bfloat162float(h0));
+    const __nv_bfloat16 l1 = __float2bfloat16(f1 - __bfloat162float(h1));
     h[j] = pack_bf16x2(h0, h1);
     l[j] = pack_bf16x2(l0, l1);
   }
@@ -302,6 +335,9 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
   if (warp < kProducerWarps) {
     // -- producers: AO rows of tile i -> [hi | lo] into A buffer i % 2 ------
     const int nitems = kM * cpk;
+    // q / cpk for q < 2^22 as the high word of q * ceil(2^32 / cpk) (cpk <= 32:
+    // the rounding excess of the multiplier stays below one quotient step)
+    const uint32_t mcpk = (uint32_t)((0x100000000ull + (uint64_t)cpk - 1) / (uint64_t)cpk);
     int i = 0;
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
       const int b = i & 1, use = i >> 1;
@@ -310,22 +346,33 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
         break;
       const int64_t row0 = tile * kM;
       unsigned char* A = smem + S.a_off[b];
-      for (int it = tid; it < nitems; it += 2 * kProducerThreads) {
-        const int it1 = it + kProducerThreads;
-        const bool two = it1 < nitems;
-        double v0[8], v1[8];
-        const int r0 = ((it >> 3) / cpk) * 8 + (it & 7), c0 = (it >> 3) % cpk;
-        const int r1 = ((it1 >> 3) / cpk) * 8 + (it1 & 7), c1 = (it1 >> 3) % cpk;
-        load8(ao, row0 + r0, nrows, nao, c0, v0);
-        if (two) load8(ao, row0 + r1, nrows, nao, c1, v1);
-        uint4 hi, lo;
-        split8(v0, hi, lo);
-        *reinterpret_cast<uint4*>(A + chunk_offset(r0, c0, S.kc)) = hi;
-        *reinterpret_cast<uint4*>(A + chunk_offset(r0, cpk + c0, S.kc)) = lo;
-        if (two) {
-          split8(v1, hi, lo);
-          *reinterpret_cast<uint4*>(A + chunk_offset(r1, c1, S.kc)) = hi;
-          *reinterpret_cast<uint4*>(A + chunk_offset(r1, cpk + c1, S.kc)) = lo;
+      // kLoadItems items per thread and iteration: their 16-byte loads are all
+      // issued before the first split, so that enough bytes are in flight
+      for (int it = tid; it < nitems; it += kLoadItems * kProducerThreads) {
+        double v[kLoadItems][8];
+        // item iu: rows 8 (q / cpk) + iu % 8, chunk q % cpk of q = iu / 8
+        auto row_of = [&](int iu) {
+          return (int)__umulhi((uint32_t)iu >> 3, mcpk) * 8 + (iu & 7);
+        };
+        auto chunk_of = [&](int iu) {
+          const uint32_t q = (uint32_t)iu >> 3;
+          return (int)(q - __umulhi(q, mcpk) * (uint32_t)cpk);
+        };
+#pragma unroll
+        for (int u = 0; u < kLoadItems; ++u) {
+          const int iu = it + u * kProducerThreads;
+          if (iu < nitems) load8(ao, row0 + row_of(iu), nrows, nao, chunk_of(iu), v[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kLoadItems; ++u) {
+          const int iu = it + u * kProducerThreads;
+          if (iu < nitems) {
+            const int r = row_of(iu), c = chunk_of(iu);
+            uint4 hi, lo;
+            split8(v[u], hi, lo);
+            *reinterpret_cast<uint4*>(A + chunk_offset(r, c, S.kc)) = hi;
+            *reinterpret_cast<uint4*>(A + chunk_offset(r, cpk + c, S.kc)) = lo;
+          }
         }
       }
       fence_proxy_async();
@@ -403,10 +450,10 @@ __global__ void __launch_bounds__(kThreads, 1) mo_tc_kernel(const double* __rest
           if (row < nrows && col < nmo) {
             double* dst = mo + row * nmo + col;
             if (vec) {  // nmo even: col + 1 < nmo and 16-byte alignment
-              *reinterpret_cast<double2*>(dst) = make_double2((double)f.x, (double)f.y);
+              *reinterpret_cast<double2*>(dst) = make_double2(f64_from_f32(f.x), f64_from_f32(f.y));
             } else {
-              dst[0] = (double)f.x;
-              if (col + 1 < nmo) dst[1] = (double)f.y;
+              dst[0] = f64_from_f32(f.x);
+              if (col + 1 < nmo) dst[1] = f64_from_f32(f.y);
             }
           }
         }
