@@ -324,6 +324,13 @@ def bench_h_n(torch, lib, device, flush, nw=16384, nstep=50):
             rel = ((wf(xs).reshape(-1) - p64) / p64).abs()
         out.setdefault("psi_rel_err_vs_fp64_median", {})["H%d" % n] = float(rel.median())
         out.setdefault("psi_rel_err_vs_fp64_p90", {})["H%d" % n] = float(torch.quantile(rel, 0.9))
+        if n % 8 == 0:  # the plain method on the chains the serving stream sends to it
+            x64 = x.clone()
+            scr64, _ = metropolis_capi(torch, lib, wf64, x64, 10, 0, STEP_SIZE, 5)
+            torch.cuda.synchronize()
+            t64 = _timed(torch, lambda i: metropolis_capi(torch, lib, wf64, x64, 10, 0, STEP_SIZE,
+                                                          6 + i, scratch=scr64), 2, flush) / 2
+            out.setdefault("fp64_walker_steps_per_s", {})["H%d" % n] = nw * 10 / t64
     return out
 
 

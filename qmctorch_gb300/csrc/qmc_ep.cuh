@@ -525,6 +525,15 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
 #pragma unroll
     for (int jj = 0; jj < JC; ++jj) a0[jj] = ad[jj] = al[jj] = (R)0;
     auto acc = [&](int a, const AOVal<R>& o) {
+      // FP64: an AO whose primitives were all cut (far atom) is zero with its
+      // derivatives, and its FMAs would add zeros: skipped (the lanes of a warp
+      // evaluate the same electron index of different walkers, so the branch
+      // is mostly uniform)
+      if constexpr (!kMixed<R>) {
+        if (o.v == (R)0 && (!KIN || (o.gx == (R)0 && o.gy == (R)0 && o.gz == (R)0 &&
+                                     o.lap == (R)0)))
+          return;
+      }
       R wv[JC];
       load_w<JC>(t.W + (int64_t)a * t.ncol + j0, wv);
       R gdot = (R)0;

@@ -189,6 +189,13 @@ def test_new_entry_points_reject_bad_arguments_without_a_gpu(name):
     assert lib.qmc_wf_gradients(ctypes.byref(desc), None, -1, 0, None, None, 0, None) == 1
     assert lib.qmc_wf_gradients(ctypes.byref(desc), ctypes.c_void_p(8), 10, 0, ctypes.c_void_p(8),
                                 ctypes.c_void_p(8), 8, None) == 3
+    # launch-plan diagnostics: argument errors before the occupancy query
+    assert lib.qmc_metropolis_plan(ctypes.byref(desc), 16, None) == 1
+    assert lib.qmc_metropolis_plan(ctypes.byref(desc), 0, (ctypes.c_int32 * 5)()) == 1
+    # the Metropolis scratch holds the walkers' positions too (split coordinates)
+    per = 3 * desc.nelec * (8 if desc.precision == 1 else 16)
+    assert (lib.qmc_metropolis_scratch_bytes(ctypes.byref(desc), 1024)
+            - lib.qmc_scratch_bytes(ctypes.byref(desc), 1024, 0)) >= per * 1024
     gb = lib.qmc_eloc_adjoint_scratch_bytes(ctypes.byref(desc), 100)
     assert gb > lib.qmc_adjoint_scratch_bytes(ctypes.byref(desc), 100) > 0
     v = ctypes.c_void_p(8)
