@@ -734,6 +734,7 @@ template <typename R, int N>
 __device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> mo, CView<R> bk,
                                        int nv, const int* tab, double* dv, double* ov, int64_t s,
                                        double* dref) {
+  static_assert(kMixed<R>, "the register local-energy path is the mixed method's");
   // LU of the occupied block (lu_factor's operations and pivots)
   R a[N][N];
 #pragma unroll
@@ -790,10 +791,23 @@ __device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> 
     R rc[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      double r = (double)(kin ? bk(i, c) : mo(i, c));
+      // residual b - A x in double-float arithmetic (an FP32 pair, about 48
+      // bits, enough for one refinement step from FP32): products split exactly
+      // by fma, sums compensated (two-sum) -- no FP64 instruction: the FP32 <->
+      // FP64 conversions of an FP64 residual issue on the FP64 pipe and hold
+      // registers
+      R sh = kin ? bk(i, c) : mo(i, c), sl = (R)0;
 #pragma unroll
-      for (int k = 0; k < N; ++k) r = fma(-(double)mo(i, k), (double)x[k], r);
-      rc[i] = (R)r;
+      for (int k = 0; k < N; ++k) {
+        const R ph = -mo(i, k) * x[k];
+        const R pl = fma(-mo(i, k), x[k], -ph);
+        const R t = sh + ph;
+        const R bb = t - sh;
+        const R err = (sh - (t - bb)) + (ph - bb);
+        sh = t;
+        sl += err + pl;
+      }
+      rc[i] = sh + sl;
     }
     apply_pivots<R, N>(piv, rc);
     lu_subst<R, N, N>(a, rc);
