@@ -796,7 +796,7 @@ def run_gb300(args):
             # (count_fp64_flops_per_psi: the work of one psi evaluation) x walker-steps
             # per launch / the launch's CUDA-event time, against the FP32 FMA rate
             # measured in this run; traffic = ncu DRAM bytes of one launch
-            "roofline": {"bound": "fp32", "kernel": "metropolis_kernel<float>",
+            "roofline": {"bound": "fp32", "kernel": "metropolis_kernel_wide<float>",
                          "achieved": ach_m / 1e3, "peak": fp32_peak / 1e3, "unit": "TFLOP/s",
                          "frac": ach_m / fp32_peak, "traffic": TRAFFIC_PER_LAUNCH,
                          "flops_per_walker_step": flops,
@@ -804,7 +804,7 @@ def run_gb300(args):
                          "launch_ms": m_met * 1e3 / args.steps,
                          "peak_source": "FP32 FMA rate measured in this run (qmc_probe_fma; "
                                         "MEASURED_PEAKS.json holds no FP32 figure)"},
-            "roofline_hbm": {"bound": "hbm", "kernel": "metropolis_kernel<float>",
+            "roofline_hbm": {"bound": "hbm", "kernel": "metropolis_kernel_wide<float>",
                              "achieved": hbm_alg / (m_met / args.steps) / 1e9,
                              "peak": hbm_peak, "unit": "GB/s",
                              "frac": hbm_alg / (m_met / args.steps) / 1e9 / hbm_peak,

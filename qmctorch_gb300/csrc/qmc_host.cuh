@@ -91,27 +91,38 @@ static inline int64_t scratch_slot_bytes(const qmc_wf_desc* d, int kind) {
 //   diagonals in FP64) keeps one thread per electron (k = 1).
 // Plans are cached per (kernel, device, walker count, shape inputs).
 template <typename R, typename K>
-static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, int64_t nw) {
+static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, int64_t nw,
+                              int bound = 0, bool* single_wave = nullptr) {
+  // bound: the kernel's threads-per-block limit (0: ep_thread_bound); single_wave
+  // (optional) receives whether the plan runs every block at once
+  if (bound <= 0) bound = ep_thread_bound<R>(kind);
   int dev = 0, nsm = 1;
   cudaGetDevice(&dev);
   const int ne = d.nelec > 0 ? d.nelec : 1;
   const EPShape s1 = ep_shape<R>(d, kind, 1, jc, ne), s2 = ep_shape<R>(d, kind, 2, jc, ne);
   struct Key {
     const void* kernel;
-    int dev, kind, jc, ne;
+    int dev, kind, jc, ne, bound;
     int64_t nw, smem1, smem2;
     bool operator==(const Key& o) const {
       return kernel == o.kernel && dev == o.dev && kind == o.kind && jc == o.jc && ne == o.ne &&
-             nw == o.nw && smem1 == o.smem1 && smem2 == o.smem2;
+             bound == o.bound && nw == o.nw && smem1 == o.smem1 && smem2 == o.smem2;
     }
   };
-  const Key key{(const void*)kernel, dev, kind, jc, ne, nw, s1.smem, s2.smem};
+  struct Plan {
+    EPShape s;
+    bool one_wave;
+  };
+  const Key key{(const void*)kernel, dev, kind, jc, ne, bound, nw, s1.smem, s2.smem};
   static std::mutex mu;
-  static std::vector<std::pair<Key, EPShape>> cache;
+  static std::vector<std::pair<Key, Plan>> cache;
   {
     std::lock_guard<std::mutex> g(mu);
     for (const auto& kv : cache)
-      if (kv.first == key) return kv.second;
+      if (kv.first == key) {
+        if (single_wave) *single_wave = kv.second.one_wave;
+        return kv.second.s;
+      }
   }
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
   int nwb0 = kMixed<R> ? 32 : 16;
@@ -136,7 +147,7 @@ static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, 
       const int nslot = (ne + k - 1) / k;
       if (k > 1 && nslot == (ne + k - 2) / (k - 1)) continue;  // same slot count as k - 1
       const EPShape s = ep_shape<R>(d, kind, nwb, jc, nslot, pg == 1);
-      if (s.nthreads > ep_thread_bound<R>(kind) || s.smem > 200 * 1024) continue;
+      if (s.nthreads > bound || s.smem > 200 * 1024) continue;
       if (prepare_smem(kernel, s.smem) != QMC_OK) continue;
       int occ = 0;
       if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, s.nthreads, s.smem) !=
@@ -161,8 +172,9 @@ static inline EPShape ep_plan(const qmc_wf_desc& d, int kind, int jc, K kernel, 
   if (best.smem >= 0) {
     std::lock_guard<std::mutex> g(mu);
     if (cache.size() > 256) cache.clear();
-    cache.emplace_back(key, best);
+    cache.emplace_back(key, Plan{best, one_wave});
   }
+  if (single_wave) *single_wave = one_wave;
   return best;
 }
 
