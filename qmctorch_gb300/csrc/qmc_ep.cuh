@@ -1158,8 +1158,12 @@ struct EPPtrs {
 
 // Evaluate psi (and, with KIN, the kinetic energy and potentials) for the
 // block's walkers at split positions `pbuf` (shared memory, [nwb][3 nelec]).
-// Results in shared memory: psi[wl], and with KIN kin[wl], v[wl] (V_en + V_ee).
-// Every thread of the block must call this (it contains block barriers).
+// Results in shared memory: psi[wl], and with KIN kin[wl], v[wl] (V_en + V_ee),
+// written by thread wl (< nwb) and visible to that thread on return: no
+// barrier follows the combine phase, so a caller reads only its own walker's
+// results, and its next write to the block's rows (positions, proposal) comes
+// after a barrier. Every thread of the block must call this (it contains block
+// barriers).
 // ELCOOP: the local-energy kernel instance with the cooperative determinant
 // phase of large channels (a separate instance: its work arrays and pivots
 // would cost the small-molecule local-energy kernel registers).
@@ -1228,7 +1232,6 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
       V[wl] = v;
     }
   }
-  __syncthreads();
 }
 
 // Stage the positions of walkers [w0, w0 + nwb) into shared memory as split
