@@ -28,6 +28,7 @@ from ..wavefunction import runtime as rt
 
 log = logging.getLogger("qmctorch_gb300")
 
+_PINNED_OUT_MAX = 256 << 20  # largest host result returned in page-locked memory (bytes)
 _MOVE = {"all-elec": 0, "one-elec": 1, "all-elec-iter": 2}
 _PROBA = {"normal": 0, "uniform": 1}
 
@@ -282,10 +283,12 @@ class Metropolis(SamplerBase):
             self._run_kernel(wf, x, device, samples=samples, nsnap=nsnap, accepted=acc,
                              replay=replay)
             self._step_counter += self.nstep
-            # the reference updates the walker tensor (and so a caller's pos) in place
+            # the reference updates the walker tensor (and so a caller's pos) in place;
+            # copy_ from the device writes a pinned host tensor by DMA, without a
+            # pageable staging copy
             wp = self.walkers.pos
             if wp.shape == x.shape:
-                wp.data.copy_(x.to(device=wp.device, dtype=wp.dtype))
+                wp.data.copy_(x if wp.dtype == x.dtype else x.to(dtype=wp.dtype))
             else:
                 self.walkers.pos = x.to(device=wp.device, dtype=out_dtype)
             if with_tqdm:
@@ -297,6 +300,12 @@ class Metropolis(SamplerBase):
                 log.info("   Total Time          : %1.2f sec.", dt)
             self._last_accepted = acc
             out = samples[:nsnap].reshape(nsnap * nw, -1)
+            if out_device.type == "cpu" and out.numel() * out.element_size() <= _PINNED_OUT_MAX:
+                # host result in page-locked memory (the host allocator caches it):
+                # one DMA instead of a staged copy
+                host = torch.empty(out.shape, dtype=out_dtype, pin_memory=True)
+                host.copy_(out if out.dtype == out_dtype else out.to(dtype=out_dtype))
+                out = host
         out = out.to(device=out_device, dtype=out_dtype)
         return self.symmetry(out).requires_grad_()
 
