@@ -399,6 +399,46 @@ int qmc_metropolis_run_batch(const qmc_wf_desc* descs, const qmc_metropolis_args
                              void* const* scratch, const int64_t* scratch_bytes, int32_t njobs,
                              void* stream);
 
+/* Arguments of qmc_drift_run (the drift-diffusion sampler). */
+typedef struct qmc_drift_args {
+  double* pos;            /* [nw][3*ne] in: start positions; out: final positions */
+  int64_t nwalkers;
+  int32_t nstep;
+  int32_t ntherm;         /* >= 0 (the caller resolves negative values) */
+  int32_t ndecor;
+  double step_size;
+  uint64_t seed;          /* Philox key */
+  uint64_t step_offset;   /* Philox counter offset (continue a chain) */
+  double* samples;        /* [nsnap][nw][3*ne] kept positions, or NULL */
+  int64_t nsnap;          /* capacity of samples in snapshots */
+  int32_t* accepted;      /* [nw] accepted moves, accumulated, or NULL */
+  /* Replay inputs: all three or none. When given they replace the generator:
+     electron_index [nstep][nw] (in [0, ne)), normals [nstep][nw][3] (the
+     proposal noise, covariance sqrt(step_size) I already applied),
+     uniforms [nstep][nw]. */
+  const int32_t* electron_index;
+  const double* normals;
+  const double* uniforms;
+} qmc_drift_args;
+
+/* Scratch bytes for qmc_drift_run. */
+int64_t qmc_drift_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
+
+/*
+ * Run nstep drift-diffusion Metropolis steps for every walker in one launch,
+ * FP64. Replaces GeneralizedMetropolis.__call__ with move / _move / trans /
+ * get_drift / _accept (generalized_metropolis.py:46-219) for the density psi^2
+ * of the described wave function: each step moves one electron e (uniform)
+ * of the call's START positions by step * drift_i(e) + eta, eta ~ N(0,
+ * sqrt(step) I), drift = grad psi / psi (Jacobi formula); accepts when
+ * min(1, T_if rho_f / (T_fi rho_i)) - u >= 0 with
+ * T(x -> y) = exp(-|y - x - step drift(x)| / (2 step)) (the norm of the whole
+ * walker vector), zero densities replaced by 1e-16. Samples are kept after
+ * ntherm steps every ndecor steps; pos receives the final positions.
+ */
+int qmc_drift_run(const qmc_wf_desc* d, const qmc_drift_args* a, void* scratch,
+                  int64_t scratch_bytes, void* stream);
+
 /*
  * Compensated statistics of x[0..n) (local energies): stats[0] = mean,
  * stats[1] = unbiased variance, stats[2] = sqrt(stats[1] / n). Replaces the

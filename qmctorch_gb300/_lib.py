@@ -23,8 +23,8 @@ BUILD = os.path.join(ROOT, "_build")
 INCLUDE = os.path.join(ROOT, "include")
 
 SOURCES = ["qmc_wf_kernels.cu", "qmc_staged.cu", "qmc_metropolis.cu", "qmc_capi_common.cu",
-           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_sweep.cu", "qmc_reduce.cu", "qmc_mo_tc.cu",
-           "qmc_scf.cpp"]
+           "qmc_probe.cu", "qmc_adjoint.cu", "qmc_drift.cu", "qmc_sweep.cu", "qmc_reduce.cu",
+           "qmc_mo_tc.cu", "qmc_scf.cpp"]
 # translation units compiled more than once, with defines: (source, object, flags)
 INSTANCES = [("qmc_metropolis_inst.cu", "qmc_metropolis_%s_%d" % (r, jc),
               ["-DQMC_INST_R=%s" % r, "-DQMC_INST_JC=%d" % jc])
@@ -125,6 +125,16 @@ class MetropolisArgs(ctypes.Structure):
     ]
 
 
+class DriftArgs(ctypes.Structure):
+    _fields_ = [
+        ("pos", c_void_p), ("nwalkers", c_int64), ("nstep", c_int32), ("ntherm", c_int32),
+        ("ndecor", c_int32), ("step_size", ctypes.c_double), ("seed", ctypes.c_uint64),
+        ("step_offset", ctypes.c_uint64), ("samples", c_void_p), ("nsnap", c_int64),
+        ("accepted", c_void_p), ("electron_index", c_void_p), ("normals", c_void_p),
+        ("uniforms", c_void_p),
+    ]
+
+
 # every symbol include/qmc_gb300.h declares: name -> (restype, argtypes)
 _P = ctypes.POINTER
 SIGNATURES = {
@@ -168,6 +178,8 @@ SIGNATURES = {
     "qmc_wf_gradients": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_int32, c_void_p,
                                         c_void_p, c_int64, c_void_p]),
     "qmc_probe_fma": (ctypes.c_int, [c_int32, c_int32, c_int64, c_void_p, c_void_p]),
+    "qmc_drift_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
+    "qmc_drift_run": (ctypes.c_int, [_P(WfDesc), _P(DriftArgs), c_void_p, c_int64, c_void_p]),
     "qmc_metropolis_run": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), c_void_p, c_int64,
                                           c_void_p]),
     "qmc_metropolis_run_batch": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), _P(c_void_p),

@@ -273,7 +273,17 @@ class Metropolis(SamplerBase):
         out_dtype = pos.dtype if pos is not None else torch.get_default_dtype()
         with torch.no_grad():
             self.walkers.initialize(pos=pos)
-            x = rt.dev64(self.walkers.pos, device).clone()
+            src = self.walkers.pos.detach()
+            if (src.device.type == "cpu" and src.is_pinned() and src.dtype == rt.F64
+                    and src.is_contiguous()):
+                # page-locked host walkers: an asynchronous DMA, ordered before
+                # the kernel on the same stream
+                x = torch.empty(src.shape, dtype=rt.F64, device=device)
+                x.copy_(src, non_blocking=True)
+            else:
+                x = rt.dev64(src, device)
+                if x.data_ptr() == src.data_ptr():
+                    x = x.clone()  # the walkers are written back below, not in the kernel
             nw = x.shape[0]
             nsnap = len(range(self.ntherm, self.nstep, self.ndecor))
             samples = torch.empty((max(nsnap, 1), nw, self.nelec * self.ndim), dtype=rt.F64,
@@ -286,9 +296,15 @@ class Metropolis(SamplerBase):
             # the reference updates the walker tensor (and so a caller's pos) in place;
             # copy_ from the device writes a pinned host tensor by DMA, without a
             # pageable staging copy
+            out = samples[:nsnap].reshape(nsnap * nw, -1)
+            pinned_out = (out_device.type == "cpu"
+                          and 0 < out.numel() * out.element_size() <= _PINNED_OUT_MAX)
             wp = self.walkers.pos
             if wp.shape == x.shape:
-                wp.data.copy_(x if wp.dtype == x.dtype else x.to(dtype=wp.dtype))
+                # into page-locked memory the copy need not wait here when the
+                # result copy below synchronises the stream
+                wp.data.copy_(x if wp.dtype == x.dtype else x.to(dtype=wp.dtype),
+                              non_blocking=pinned_out and wp.is_pinned())
             else:
                 self.walkers.pos = x.to(device=wp.device, dtype=out_dtype)
             if with_tqdm:
@@ -299,8 +315,7 @@ class Metropolis(SamplerBase):
                 log.info("   Timing statistics   : %1.2f steps/sec.", self.nstep / dt)
                 log.info("   Total Time          : %1.2f sec.", dt)
             self._last_accepted = acc
-            out = samples[:nsnap].reshape(nsnap * nw, -1)
-            if out_device.type == "cpu" and out.numel() * out.element_size() <= _PINNED_OUT_MAX:
+            if pinned_out:
                 # host result in page-locked memory (the host allocator caches it):
                 # one DMA instead of a staged copy
                 host = torch.empty(out.shape, dtype=out_dtype, pin_memory=True)

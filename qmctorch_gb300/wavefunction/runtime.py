@@ -95,6 +95,77 @@ def jastrow_parts(jastrow):
     return (ee[0] if ee else None), (en[0] if en else None)
 
 
+def desc_sources(ao, mo=None, jastrow=None, fc=None):
+    """The tensors whose values ``build_desc`` copies into a descriptor or
+    points it at, in a fixed order."""
+    src = [ao.atom_coords, ao.bas_exp]
+    if mo is not None:
+        src += [mo.mo_scf, mo.mo_modifier]
+    ee, en = jastrow_parts(jastrow)
+    if ee is not None:
+        src.append(ee.jastrow_kernel.weight)
+    if en is not None:
+        src += [en.jastrow_kernel.weight, en.atoms]
+    if fc is not None:
+        src.append(fc.weight)
+    return src
+
+
+class DescMemo:
+    """The last descriptor built for a wave function and what it was built
+    from, so that repeated calls with unchanged parameters make no
+    host-to-device copies. A host tensor is compared by value with a snapshot
+    taken at build time (a write through ``.data`` does not advance a tensor's
+    version counter, so versions are not trusted); a device FP64 contiguous
+    tensor is used in place by the descriptor, so its identity and storage
+    address are compared; a descriptor built from any other source (a device
+    tensor that needed a conversion) is never reused."""
+
+    def __init__(self):
+        self.key = None
+        self.snap = None
+        self.call = None
+
+    def __deepcopy__(self, memo):
+        return DescMemo()
+
+    def __getstate__(self):
+        return {"key": None, "snap": None, "call": None}
+
+    @staticmethod
+    def _snapshot(t, device):
+        t = t.detach()
+        if t.device.type == "cpu":
+            return t.clone()
+        if t.device == device and t.dtype == F64 and t.is_contiguous():
+            return t.data_ptr()
+        return None
+
+    def get(self, key, sources, device):
+        if self.call is None or key != self.key or len(sources) != len(self.snap):
+            return None
+        for t, (ref, s) in zip(sources, self.snap):
+            if t is not ref:
+                return None
+            if isinstance(s, torch.Tensor):
+                td = t.detach()
+                if td.device.type != "cpu" or td.dtype != s.dtype or td.shape != s.shape or \
+                        not torch.equal(td, s):
+                    return None
+            elif (t.device != device or t.dtype != F64 or not t.is_contiguous()
+                  or t.data_ptr() != s):
+                return None
+        return self.call
+
+    def put(self, key, sources, device, call):
+        snap = [(t, self._snapshot(t, device)) for t in sources]
+        if any(s is None for _, s in snap):
+            self.key = self.snap = self.call = None
+        else:
+            self.key, self.snap, self.call = key, snap, call
+        return call
+
+
 def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None, nup=None,
                ndown=None, nmo_used=None, e_nuc=0.0, precision=0):
     """Fill a ``qmc_wf_desc`` from the modules of a wave function. Any module
@@ -110,6 +181,7 @@ def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None
     d.natom = ao.natoms
     d.nao = ao.norb
     bt = ao.device_tables(device)
+    keep.append(bt)  # its index tensors are pointed at by the descriptor
     coords = dev64(ao.atom_coords, device)
     charge = ao.atomic_charge(device)
     bexp = dev64(ao.bas_exp, device)
@@ -156,6 +228,7 @@ def build_desc(device, ao, mo=None, pool=None, jastrow=None, fc=None, nelec=None
         d.jastrow_en_w = d.jastrow_en_atoms = ptr(dd)
     if pool is not None:
         ct = pool.device_tables(device)
+        keep.append(ct)
         d.det_mode = 1 if ct.explicit else 0
         d.ncfg = ct.ncfg
         d.max_orb[0], d.max_orb[1] = ct.max_orb

@@ -180,6 +180,7 @@ class SlaterJastrow(WaveFunction):
         self.gradients = self.gradients_jacobi
         self.kinetic_energy = self.kinetic_energy_jacobi
         self._enuc_cache = (None, 0.0)
+        self._desc_memo = rt.DescMemo()
         self._no_jastrow_w = torch.zeros(1)
         if cuda:
             self.device = rt.cuda_device()
@@ -188,23 +189,35 @@ class SlaterJastrow(WaveFunction):
     # -- descriptors ----------------------------------------------------------
     def nuclear_repulsion(self):
         """V_nn (wf_base.py:97-116)."""
-        key = (self.ao.atom_coords._version, self.ao.atom_coords.data_ptr())
-        if self._enuc_cache[0] != key:
-            c = self.ao.atom_coords.detach().to("cpu", torch.float64)
+        c = self.ao.atom_coords.detach().to("cpu", torch.float64)
+        if self._enuc_cache[0] is None or not torch.equal(self._enuc_cache[0], c):
             z = self.ao.atomic_number
             v = 0.0
             for a in range(self.natom - 1):
                 for b in range(a + 1, self.natom):
                     v += z[a] * z[b] / float(torch.sqrt(((c[a] - c[b]) ** 2).sum()))
-            self._enuc_cache = (key, v)
+            self._enuc_cache = (c, v)
         return self._enuc_cache[1]
 
     def _desc(self, device):
-        return rt.build_desc(device, self.ao, mo=self.mo, pool=self.pool,
-                             jastrow=self.jastrow if self.use_jastrow else None, fc=self.fc,
-                             nup=self.mol.nup, ndown=self.mol.ndown,
+        """The kernels' descriptor of this wave function on ``device``: the
+        last one built while its parameters keep the values it was built from
+        (``rt.DescMemo``), else a new one."""
+        jastrow = self.jastrow if self.use_jastrow else None
+        key = (str(device), self.precision, self.highest_occ_mo, self.mol.nup, self.mol.ndown,
+               id(self.ao), id(self.mo), id(self.pool), id(jastrow), id(self.fc))
+        src = rt.desc_sources(self.ao, mo=self.mo, jastrow=jastrow, fc=self.fc)
+        memo = self.__dict__.get("_desc_memo")
+        if memo is None:
+            memo = self._desc_memo = rt.DescMemo()
+        call = memo.get(key, src, device)
+        if call is not None:
+            return call
+        call = rt.build_desc(device, self.ao, mo=self.mo, pool=self.pool, jastrow=jastrow,
+                             fc=self.fc, nup=self.mol.nup, ndown=self.mol.ndown,
                              nmo_used=self.highest_occ_mo, e_nuc=self.nuclear_repulsion(),
                              precision=PRECISIONS[self.precision])
+        return memo.put(key, src, device, call)
 
     # -- fused evaluations ----------------------------------------------------
     def _psi(self, pos):

@@ -244,3 +244,59 @@ def test_pipeline_wait_limit_is_host_settable_without_a_gpu():
     finally:
         lib.qmc_set_wait_limit_ns(old)
     assert lib.qmc_status_string(7).startswith(b"a bounded pipeline wait")
+
+
+def test_descriptor_is_reused_only_while_its_sources_keep_their_values():
+    """SlaterJastrow._desc returns the descriptor it built last while every
+    tensor it was built from is the same object with the same values, and
+    builds a new one after any change, including writes through ``.data``
+    (which leave a tensor's version counter alone)."""
+    mol = Molecule("H 0 0 0; H 0 0 0.74", unit="angs", basis="sto-3g", calculator="huckel")
+    wf = SlaterJastrow(mol, configs="single_double(2,2)")
+    dev = torch.device("cpu")
+    c1 = wf._desc(dev)
+    assert wf._desc(dev) is c1
+    wf.fc.weight.data[0][1] = 0.25  # no version change
+    c2 = wf._desc(dev)
+    assert c2 is not c1
+    w = ctypes.cast(c2.desc.ci_weight, ctypes.POINTER(ctypes.c_double))
+    assert w[1] == 0.25
+    with torch.no_grad():
+        wf.jastrow.jastrow_kernel.weight.add_(0.5)
+    c3 = wf._desc(dev)
+    assert c3 is not c2
+    jw = ctypes.cast(c3.desc.jastrow_w, ctypes.POINTER(ctypes.c_double))
+    assert jw[0] == float(wf.jastrow.jastrow_kernel.weight.detach())
+    wf.mo.mo_scf = torch.nn.Parameter(wf.mo.mo_scf.detach().clone() * 2.0)
+    c4 = wf._desc(dev)
+    assert c4 is not c3
+    assert wf._desc(dev) is c4
+    wf.ao.atom_coords.data[1, 2] += 0.1  # geometry: V_nn follows
+    c5 = wf._desc(dev)
+    assert c5 is not c4 and c5.desc.e_nuc != c4.desc.e_nuc
+
+
+@pytest.mark.parametrize("name", ["h2o_sd", "lih_cas"])
+def test_drift_sampler_rejects_bad_arguments_without_a_gpu(name):
+    """qmc_drift_run checks its arguments (step, decorrelation, replay inputs
+    all or none, snapshot buffer, scratch size) before any device call; an
+    empty run is a no-op."""
+    lib = _lib.lib()
+    desc, keep, wf = _desc_for(name)
+    v = ctypes.c_void_p(8)
+    a = _lib.DriftArgs()
+    a.pos, a.nwalkers, a.nstep, a.ntherm, a.ndecor, a.step_size = v, 16, 4, 0, 1, 0.2
+    need = lib.qmc_drift_scratch_bytes(ctypes.byref(desc), 16)
+    assert need > 0 and lib.qmc_drift_scratch_bytes(ctypes.byref(desc), 1024) > need
+    assert lib.qmc_drift_run(ctypes.byref(desc), None, v, need, None) == 1
+    assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), v, need - 8, None) == 3
+    a.step_size = 0.0
+    assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.step_size, a.ndecor = 0.2, 0
+    assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.ndecor, a.normals = 1, v  # replay needs all three inputs
+    assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.normals, a.nsnap = None, 2  # snapshots without a buffer
+    assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.nsnap, a.nstep = 0, 0
+    assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), None, 0, None) == 0
