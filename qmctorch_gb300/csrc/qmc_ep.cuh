@@ -612,7 +612,7 @@ __device__ inline double lu_solve_regs(R* rows, int64_t rs, int64_t cs, int nv) 
     }
     if (p != k) det = -det;
     const R akk = a[k][k];
-    det *= (double)akk;
+    det *= to_f64(akk);
     const R inv = akk != (R)0 ? (R)1 / akk : (R)0;
     a[k][k] = inv;
 #pragma unroll
@@ -768,7 +768,7 @@ __device__ inline void el_channel_regs(const qmc_wf_desc& d, int spin, CView<R> 
     }
     if (p != k) det = -det;
     const R akk = a[k][k];
-    det *= (double)akk;
+    det *= to_f64(akk);
     const R inv = akk != (R)0 ? (R)1 / akk : (R)0;
     a[k][k] = inv;
 #pragma unroll
@@ -1008,7 +1008,7 @@ __device__ inline double coop_lu_steps(R* A, int64_t rs, int64_t cs, int n, int 
       const R akk = A[k * rs + k * cs];
       piv[k] = p;
       if (p != k) det = -det;
-      det *= (double)akk;
+      det *= to_f64(akk);
       inv = akk != (R)0 ? (R)1 / akk : (R)0;
       for (int i = k + 1 + r; i < n; i += nt) {
         const R l = A[i * rs + k * cs] * inv;
@@ -1220,13 +1220,19 @@ __device__ inline void ep_eval(const qmc_wf_desc& d, const Tables<R>& t, const E
     const int64_t slot = dsm ? wl : w;
     const T* dv = rptr<T>(dbase, L.dv, dss, slot);
     const double* ov = KIN ? rptr<double>(dbase, L.ov, dss, slot) : nullptr;
-    const double psid = ci_combine<T, KIN, T>(d, dv, ov, dss, DREF[wl], DREF[nwb + wl], &kin);
+    const double psid = ci_combine<T, KIN, T>(d, dv, ov, dss, DREF[wl], DREF[nwb + wl], &kin,
+                                               (!KIN && kMixed<R>) ? (const T*)t.ciw : nullptr);
     double logj = 0.0, v = 0.0;
     for (int e = 0; e < ne; ++e) {
       logj += JR[e * nwb + wl];
       if (KIN) v += VR[e * nwb + wl];
     }
-    PSI[wl] = (d.use_jastrow || d.use_jastrow_en) ? psid * exp(logj) : psid;
+    double jf = 1.0;
+    if (d.use_jastrow || d.use_jastrow_en) {
+      if constexpr (kMixed<R> && !KIN) jf = exp_mixed(logj);
+      else jf = exp(logj);
+    }
+    PSI[wl] = psid * jf;
     if (KIN) {
       KINV[wl] = kin;
       V[wl] = v;
@@ -1268,7 +1274,7 @@ __device__ __forceinline__ XP<R> xp_add(XP<R> x, R dz, R dl = (R)0) {
 
 template <typename R>
 __device__ __forceinline__ double xp_value(XP<R> x) {
-  return (double)x.h + (double)x.l;
+  return to_f64(x.h) + to_f64(x.l);
 }
 
 }  // namespace qmc

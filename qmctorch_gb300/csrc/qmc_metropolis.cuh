@@ -128,9 +128,17 @@ __device__ __forceinline__ void metropolis_block(const qmc_wf_desc& d, const qmc
         }
         double fxn = PSI[tid] * PSI[tid];
         if (fxn == 0.0) fxn = eps;
-        double df = fxn / F[tid];
-        if (df > 1.0) df = 1.0;
-        const int acc = (df - u >= 0.0) ? 1 : 0;
+        int acc;
+        if constexpr (kMixed<R>) {
+          // min(1, fxn / F) - u >= 0 for u in [0, 1) without the FP64 division
+          // (a sequence of FP64 instructions in the single-warp phase): the
+          // same decision up to the rounding of the ratio
+          acc = fxn >= u * F[tid] ? 1 : 0;
+        } else {
+          double df = fxn / F[tid];
+          if (df > 1.0) df = 1.0;
+          acc = (df - u >= 0.0) ? 1 : 0;
+        }
         ACC[tid] = acc;
         if (acc) {
           F[tid] = fxn;

@@ -163,34 +163,8 @@ __device__ inline uint32_t pack_bf16x2(__nv_bfloat16 a, __nv_bfloat16 b) {
   return (uint32_t)__bfloat16_as_ushort(a) | ((uint32_t)__bfloat16_as_ushort(b) << 16);
 }
 
-// FP64 -> FP32 by integer operations on the bit pattern, truncating the
-// mantissa (relative error below 2^-23; the split keeps 16 bits): exponent
-// rebiased, values below FP32's normal range to a signed zero, above it to
-// infinity. No instruction on the FP64 pipe, which a conversion instruction
-// would occupy at the FP64 rate.
-__device__ __forceinline__ float f32_trunc(double x) {
-  const int hi = __double2hiint(x);
-  const unsigned lo = (unsigned)__double2loint(x);
-  const int e = ((hi >> 20) & 0x7FF) - 896;  // 1023 - 127
-  const unsigned m = ((unsigned)(hi & 0xFFFFF) << 3) | (lo >> 29);
-  const unsigned s = (unsigned)hi & 0x80000000u;
-  const unsigned bits = e <= 0 ? s : (e >= 255 ? (s | 0x7F800000u) : (s | ((unsigned)e << 23) | m));
-  return __uint_as_float(bits);
-}
-
-// FP32 -> FP64 by integer operations on the bit pattern, without branches
-// (the conversion instruction issues on the FP64 pipe): exact for normal
-// values, infinity and NaN; zero and subnormal values (below 1.2e-38) give a
-// signed zero.
-__device__ __forceinline__ double f64_from_f32(float f) {
-  const unsigned b = __float_as_uint(f);
-  const unsigned e = (b >> 23) & 0xFFu;
-  const unsigned s = b & 0x80000000u;
-  const unsigned ee = e == 255u ? 2047u : e + 896u;
-  const unsigned hi = e == 0u ? s : (s | (ee << 20) | ((b & 0x7FFFFFu) >> 3));
-  const unsigned lo = e == 0u ? 0u : (b << 29);
-  return __hiloint2double((int)hi, (int)lo);
-}
+// f32_trunc and f64_from_f32 (integer conversions that keep the FP64 pipe
+// free) are shared with the fused kernels: qmc_device.cuh.
 
 // Split 8 FP64 values into their BF16 hi and lo parts, packed as 16 bytes each.
 // The split runs in FP32 (x truncated to FP32 first: its 24 bits hold the 16
