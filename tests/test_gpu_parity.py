@@ -83,6 +83,36 @@ def test_staged_modules(name):
     close(wf(pos, ao=ao), d["psi"], rtol=1e-9)
 
 
+def test_staged_modules_c6h6_against_the_oracle():
+    """The module path on C6H6 cc-pVDZ (42 electrons, 120 AOs; its fixture
+    keeps no AO arrays) against the oracle on the fixture's positions plus
+    fresh ones: AO values, gradients (per axis and summed) and laplacians, MO
+    values, the Jastrow factor with its derivatives, the determinants and psi."""
+    mol, d = load("c6h6")
+    wf = make_wf(mol, d)
+    ow = orc.OracleSlaterJastrow(mol, configs=d["configs"], include_all_mo=d["include_all_mo"],
+                                 fc_weight=d["fc_weight"])
+    rng = np.random.default_rng(5)
+    pos = np.concatenate([d["pos"], d["pos"] + 0.2 * rng.normal(size=d["pos"].shape)])
+    x = torch.as_tensor(pos).cuda()
+    ao_r, dao_r, d2ao_r = orc.ao_values(ow.basis, pos, [0, 1, 2])
+    ao, dao, d2ao = wf.ao(x, derivative=[0, 1, 2])
+    close(ao, ao_r)
+    close(dao, dao_r)
+    close(d2ao, d2ao_r)
+    close(wf.ao(x, derivative=1), orc.ao_values(ow.basis, pos, 1))
+    mo = wf.mo(ao)
+    mo_r = ao_r @ ow.W
+    close(mo, mo_r)
+    j, dj, d2j = wf.jastrow(x, derivative=[0, 1, 2], sum_grad=False)
+    j_r, dj_r, d2j_r = ow.jastrow(pos, derivative=[0, 1, 2], sum_grad=False)
+    close(j, j_r)
+    close(dj, dj_r)
+    close(d2j, d2j_r)
+    close(wf.pool(mo), ow.pool.dets(mo_r), rtol=1e-9)
+    close(wf(x, ao=ao), ow.forward(pos), rtol=1e-9)
+
+
 @pytest.mark.parametrize("name", CASES)
 def test_psi_matches_oracle_on_fresh_positions(name):
     mol, d = load(name)
