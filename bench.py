@@ -194,7 +194,8 @@ def probe_peaks(torch, lib, device):
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     res = {}
     for kind, name, iters, per in ((0, "fp64_gflops", 2000, 16), (1, "fp32_gflops", 20000, 16),
-                                   (2, "fp32_exp_gps", 10000, 8), (3, "fp64_exp_gps", 100, 8)):
+                                   (2, "fp32_exp_gps", 10000, 8), (3, "fp64_exp_gps", 100, 8),
+                                   (4, "fp64_exp_table_gps", 100, 8)):
         lib.qmc_probe_fma(kind, blocks, iters, ctypes.c_void_p(out.data_ptr()), stream)
         torch.cuda.synchronize()
         best = 0.0

@@ -178,6 +178,7 @@ SIGNATURES = {
     "qmc_wf_gradients": (ctypes.c_int, [_P(WfDesc), c_void_p, c_int64, c_int32, c_void_p,
                                         c_void_p, c_int64, c_void_p]),
     "qmc_probe_fma": (ctypes.c_int, [c_int32, c_int32, c_int64, c_void_p, c_void_p]),
+    "qmc_probe_exp64": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_drift_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
     "qmc_drift_run": (ctypes.c_int, [_P(WfDesc), _P(DriftArgs), c_void_p, c_int64, c_void_p]),
     "qmc_metropolis_run": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), c_void_p, c_int64,

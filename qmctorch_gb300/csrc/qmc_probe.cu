@@ -4,6 +4,7 @@
 #include <stdint.h>
 
 #include "../../include/qmc_gb300_probe.h"
+#include "qmc_device.cuh"
 
 template <typename T>
 __global__ void __launch_bounds__(256) fma_probe(int64_t iters, double* out) {
@@ -22,7 +23,7 @@ __global__ void __launch_bounds__(256) fma_probe(int64_t iters, double* out) {
   out[tid] = (double)s;
 }
 
-template <typename T>
+template <typename T, bool TANG = false>
 __global__ void __launch_bounds__(256) exp_probe(int64_t iters, double* out) {
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
   T a[8];
@@ -33,6 +34,8 @@ __global__ void __launch_bounds__(256) exp_probe(int64_t iters, double* out) {
     for (int k = 0; k < 8; ++k) {
       if constexpr (sizeof(T) == 4)
         a[k] = -__expf(a[k]) * (T)1e-3;
+      else if (TANG)
+        a[k] = -qmc::exp_tang(a[k]) * (T)1e-3;
       else
         a[k] = -exp(a[k]) * (T)1e-3;
     }
@@ -45,11 +48,25 @@ __global__ void __launch_bounds__(256) exp_probe(int64_t iters, double* out) {
 
 extern "C" int qmc_probe_fma(int32_t kind, int32_t blocks, int64_t iters, double* out,
                              void* stream) {
-  if (blocks <= 0 || iters <= 0 || !out || kind < 0 || kind > 3) return 1;
+  if (blocks <= 0 || iters <= 0 || !out || kind < 0 || kind > 4) return 1;
   cudaStream_t s = (cudaStream_t)stream;
   if (kind == 0) fma_probe<double><<<blocks, 256, 0, s>>>(iters, out);
   if (kind == 1) fma_probe<float><<<blocks, 256, 0, s>>>(iters, out);
   if (kind == 2) exp_probe<float><<<blocks, 256, 0, s>>>(iters, out);
   if (kind == 3) exp_probe<double><<<blocks, 256, 0, s>>>(iters, out);
+  if (kind == 4) exp_probe<double, true><<<blocks, 256, 0, s>>>(iters, out);
+  return cudaGetLastError() == cudaSuccess ? 0 : 4;
+}
+
+__global__ void __launch_bounds__(256) exp64_eval(const double* __restrict__ x, int64_t n,
+                                                  double* __restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) y[i] = qmc::rexp(x[i]);
+}
+
+extern "C" int qmc_probe_exp64(const double* x, int64_t n, double* y, void* stream) {
+  if (n < 0 || (n > 0 && (!x || !y))) return 1;
+  if (n == 0) return 0;
+  exp64_eval<<<(unsigned)((n + 255) / 256), 256, 0, (cudaStream_t)stream>>>(x, n, y);
   return cudaGetLastError() == cudaSuccess ? 0 : 4;
 }
