@@ -7,9 +7,10 @@
   same seed and initial walkers (tests/golden/gmetropolis.npz). Tolerance:
   1e-9 absolute on the positions (FP64 density and drift agree with the
   reference's to about 1e-14; the accept / reject decisions are the same).
-* On H2O cc-pVDZ single_double(4,4) the kernel is compared with this package's
-  host loop (density by qmc_wf_psi, drift by qmc_wf_gradients) on the same
-  draws: same tolerance.
+* On H2O cc-pVDZ single_double(4,4), LiH cas(2,2), their electron-nucleus and
+  combined Jastrow cases and LiH with Slater-type orbitals the kernel is compared
+  with this package's host loop (density by qmc_wf_psi, drift by
+  qmc_wf_gradients) on the same draws: same tolerance.
 * With the device generator the chains are reproducible, keep the proposal
   rule (a kept position differs from the call's start positions in at most
   one electron), and accept at the rate of the torch-drawn chains.
@@ -21,6 +22,7 @@ import pytest
 import torch
 
 from tests.golden_cases import load
+from tests.golden_cases import make_wf as golden_make_wf
 
 pytestmark = pytest.mark.gpu
 
@@ -28,12 +30,9 @@ GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "gme
 
 
 def make_wf(name):
-    from qmctorch_gb300.wavefunction import SlaterJastrow
-    torch.set_default_dtype(torch.float64)
+    """The case's wave function (its Jastrow factors: e-e, e-n or both; GTO or STO)."""
     mol, d = load(name)
-    wf = SlaterJastrow(mol, configs=d["configs"], include_all_mo=d["include_all_mo"], cuda=True)
-    wf.fc.weight.data = torch.as_tensor(d["fc_weight"]).reshape(1, -1).to(wf.fc.weight.device)
-    return mol, d, wf
+    return mol, d, golden_make_wf(mol, d)
 
 
 class HostLoopPdf:
@@ -66,7 +65,7 @@ def test_drift_sampler_chains_match_the_reference_on_h2():
     np.testing.assert_allclose(s.walkers.pos.cpu().numpy(), g["h2_final"], rtol=0, atol=1e-9)
 
 
-@pytest.mark.parametrize("name", ["h2o_sd", "lih_cas"])
+@pytest.mark.parametrize("name", ["h2o_sd", "lih_cas", "h2o_en", "lih_en", "lih_sto"])
 def test_drift_kernel_matches_the_host_loop(name):
     from qmctorch_gb300.sampler import GeneralizedMetropolis
     mol, d, wf = make_wf(name)
