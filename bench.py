@@ -68,7 +68,7 @@ def parse():
     p.add_argument("--serve-budget-gb", type=int, default=32)
     p.add_argument("--skip", default="",
                    help="comma list of sections to leave out (c6h6, serving, small, modules, "
-                        "mo_tc, h_n, precision, drift, e2e); for short profiling runs")
+                        "mo_tc, h_n, precision, drift, hmc, e2e); for short profiling runs")
     p.add_argument("--c6h6-sweeps", type=int, default=4,
                    help="all-elec-iter sweeps per timed C6H6 launch (mixed method)")
     p.add_argument("--mc-steps", type=int, default=100)
@@ -487,6 +487,40 @@ def bench_drift(torch, wf, x_eq, nstep_kernel=50, nstep_loop=5):
     return out
 
 
+def bench_hmc(torch, wf, x_eq, nstep_kernel=10, nstep_loop=2, traj=5):
+    """HMC sampler (Hamiltonian) on H2O cc-pVDZ single_double(4,4), FP64, the
+    walkers of the headline, trajectories of 5 leapfrog steps: one qmc_hmc_run
+    launch per call (device generator) against the host loop of one density
+    and one gradient kernel call per leapfrog point, both through
+    Hamiltonian.__call__ from device walkers. Unit: walker-trajectories/s."""
+    from qmctorch_gb300.sampler import Hamiltonian
+
+    class HostLoopPdf:  # wf.pdf under another name: the sampler's host loop
+        def __init__(self, wf):
+            self.__self__, self.__name__ = wf, "pdf_host_loop"
+
+        def __call__(self, x, return_grad=False):
+            return self.__self__.pdf(x, return_grad=return_grad)
+
+    nw = x_eq.shape[0]
+    out = {"workload": "h2o_ccpvdz_sd44_%dw_fp64_L%d" % (nw, traj)}
+    for name, pdf, nstep in (("kernel", wf.pdf, nstep_kernel),
+                             ("host_loop", HostLoopPdf(wf), nstep_loop)):
+        s = Hamiltonian(nwalkers=nw, nstep=nstep, step_size=0.02, L=traj, ntherm=-1,
+                        nelec=wf.mol.nelec, ndim=3, cuda=True, seed=19)
+        s(pdf, pos=x_eq.clone(), with_tqdm=False)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s(pdf, pos=x_eq.clone(), with_tqdm=False)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[name] = {"nstep": nstep, "wall_s": dt, "walker_trajectories_per_s": nw * nstep / dt,
+                     "acceptance": s.last_acceptance}
+    out["speedup"] = (out["kernel"]["walker_trajectories_per_s"]
+                      / out["host_loop"]["walker_trajectories_per_s"])
+    return out
+
+
 def bench_staged(torch, wf, x, flush):
     """The module kernels a caller of a single layer gets (wf.ao, wf.mo,
     wf.jastrow; FP64, reference tensor layouts) on the bench walkers:
@@ -774,6 +808,7 @@ def run_gb300(args):
     small = bench_h2_lih(torch, device) if rank == 0 and "small" not in skip else None
     staged = bench_staged(torch, wf64, x_eq, flush) if rank == 0 and "modules" not in skip else None
     drift = bench_drift(torch, wf64, x_eq) if rank == 0 and "drift" not in skip else None
+    hmc = bench_hmc(torch, wf64, x_eq) if rank == 0 and "hmc" not in skip else None
     mo_tc = (bench_mo_tensor_core(torch, device, flush)
              if rank == 0 and "mo_tc" not in skip else None)
     h_n = bench_h_n(torch, lib, device, flush) if rank == 0 and "h_n" not in skip else None
@@ -859,6 +894,7 @@ def run_gb300(args):
             "small_configs": small,
             "module_kernels": staged,
             "drift_sampler": drift,
+            "hmc_sampler": hmc,
             "mo_tensor_core": mo_tc,
             "h_n_metropolis": h_n,
             "precision_vs_fp64": prec,

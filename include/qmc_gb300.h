@@ -439,6 +439,41 @@ int64_t qmc_drift_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
 int qmc_drift_run(const qmc_wf_desc* d, const qmc_drift_args* a, void* scratch,
                   int64_t scratch_bytes, void* stream);
 
+/* Arguments of qmc_hmc_run (Hamiltonian Monte Carlo). */
+typedef struct qmc_hmc_args {
+  double* pos;            /* [nw][3*ne] in: start positions; out: final positions */
+  int64_t nwalkers;
+  int32_t nstep;
+  int32_t ntherm;         /* >= 0 (the caller resolves negative values) */
+  int32_t ndecor;
+  int32_t traj_length;    /* leapfrog steps per trajectory (L >= 1) */
+  double step_size;       /* leapfrog step eps */
+  uint64_t seed;          /* Philox key */
+  uint64_t step_offset;   /* Philox counter offset (continue a chain) */
+  double* samples;        /* [nsnap][nw][3*ne] kept positions, or NULL */
+  int64_t nsnap;          /* capacity of samples in snapshots */
+  int32_t* accepted;      /* [nw] accepted trajectories, accumulated, or NULL */
+  /* Replay inputs: both or none. momenta [nstep][nw][3*ne] (standard normal),
+     uniforms [nstep][nw]. */
+  const double* momenta;
+  const double* uniforms;
+} qmc_hmc_args;
+
+/* Scratch bytes for qmc_hmc_run. */
+int64_t qmc_hmc_scratch_bytes(const qmc_wf_desc* d, int64_t nwalkers);
+
+/*
+ * Run nstep Hamiltonian Monte Carlo steps for every walker in one launch,
+ * FP64. Replaces Hamiltonian.__call__ with _step (hamiltonian.py:75-201) for
+ * the density psi^2 of the described wave function: momenta p ~ N(0, I),
+ * H = -log psi^2 + |p|^2 / 2, a leapfrog trajectory of traj_length steps of
+ * size step_size with the force 2 grad psi / psi (Jacobi formula), the end
+ * point rejected when exp(H_start - H_end) < u. Samples are kept after ntherm
+ * steps every ndecor steps; pos receives the final positions.
+ */
+int qmc_hmc_run(const qmc_wf_desc* d, const qmc_hmc_args* a, void* scratch,
+                int64_t scratch_bytes, void* stream);
+
 /*
  * Compensated statistics of x[0..n) (local energies): stats[0] = mean,
  * stats[1] = unbiased variance, stats[2] = sqrt(stats[1] / n). Replaces the

@@ -135,6 +135,16 @@ class DriftArgs(ctypes.Structure):
     ]
 
 
+class HmcArgs(ctypes.Structure):
+    _fields_ = [
+        ("pos", c_void_p), ("nwalkers", c_int64), ("nstep", c_int32), ("ntherm", c_int32),
+        ("ndecor", c_int32), ("traj_length", c_int32), ("step_size", ctypes.c_double),
+        ("seed", ctypes.c_uint64), ("step_offset", ctypes.c_uint64), ("samples", c_void_p),
+        ("nsnap", c_int64), ("accepted", c_void_p), ("momenta", c_void_p),
+        ("uniforms", c_void_p),
+    ]
+
+
 # every symbol include/qmc_gb300.h declares: name -> (restype, argtypes)
 _P = ctypes.POINTER
 SIGNATURES = {
@@ -181,6 +191,8 @@ SIGNATURES = {
     "qmc_probe_exp64": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p]),
     "qmc_drift_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
     "qmc_drift_run": (ctypes.c_int, [_P(WfDesc), _P(DriftArgs), c_void_p, c_int64, c_void_p]),
+    "qmc_hmc_scratch_bytes": (c_int64, [_P(WfDesc), c_int64]),
+    "qmc_hmc_run": (ctypes.c_int, [_P(WfDesc), _P(HmcArgs), c_void_p, c_int64, c_void_p]),
     "qmc_metropolis_run": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), c_void_p, c_int64,
                                           c_void_p]),
     "qmc_metropolis_run_batch": (ctypes.c_int, [_P(WfDesc), _P(MetropolisArgs), _P(c_void_p),

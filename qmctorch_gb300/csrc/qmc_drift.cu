@@ -1,5 +1,7 @@
-// Drift-diffusion (generalized) Metropolis on the device, FP64, one thread per
-// walker for all steps of a call (generalized_metropolis.py:46-219).
+// Drift-diffusion (generalized) Metropolis and Hamiltonian Monte Carlo on the
+// device, FP64, one thread per walker for all steps of a call
+// (generalized_metropolis.py:46-219, hamiltonian.py:75-201); the HMC kernel is
+// at the end of the file.
 //
 // The reference's chain, kept as it is so that replayed draws give its chains:
 // every proposal starts from the walkers' positions at the start of the call
@@ -134,6 +136,89 @@ __device__ __forceinline__ void pade_pair(double w0, double w, const double (&xi
   for (int q = 0; q < 3; ++q) g[q] += w0 * iu * iu * dx[q] / r;
 }
 
+// Sum over the CI configurations: returns Sigma = sum_k c_k D_k^up D_k^dn and
+// writes grad Sigma (the Jacobi traces weighted by each configuration) to
+// sw[(out + c) * ss]; the moved spin sm's determinants come from dvf / gdf
+// (sm < 0: none moved), the others from dv0 / gd0.
+__device__ inline double drift_slater(const qmc_wf_desc& d, const DriftLayout& L, double* sw,
+                                      int64_t ss, int sm, int64_t out) {
+  const int nc = 3 * d.nelec, nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  auto S = [&](int64_t item) -> double& { return sw[item * ss]; };
+  for (int c = 0; c < nc; ++c) S(out + c) = 0.0;
+  double sigma = 0.0;
+  for (int k = 0; k < d.ncfg; ++k) {
+    const int uu = __ldg(d.cfg_det[0] + k), ud = __ldg(d.cfg_det[1] + k);
+    const int k0 = uu, k1 = d.ndet[0] + ud;
+    const double dv0 = S((sm == 0 ? L.dvf : L.dv0) + k0);
+    const double dv1 = S((sm == 1 ? L.dvf : L.dv0) + k1);
+    const double cd = __ldg(d.ci_weight + k) * dv0 * dv1;
+    sigma += cd;
+    for (int s = 0; s < 2; ++s) {
+      const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0, kk = s ? k1 : k0;
+      const int64_t gd = (s == sm ? L.gdf : L.gd0) + (int64_t)kk * nmax * 3;
+      for (int i = 0; i < n; ++i)
+        for (int q = 0; q < 3; ++q)
+          S(out + 3 * (r0 + i) + q) = fma(cd, S(gd + i * 3 + q), S(out + 3 * (r0 + i) + q));
+    }
+  }
+  return sigma;
+}
+
+// Full evaluation at positions P (coordinate c at P[c * ps]): the MO rows and
+// their gradients into ma..mz, the spin determinants and their electron
+// gradients into dv0 / gd0, the Jastrow gradient into jg0, and
+// grad log psi = grad Sigma / Sigma + grad log J into sw[(out + c) * ss].
+// Returns Sigma; *logj = log J.
+__device__ inline double drift_full_eval(const qmc_wf_desc& d, const Tables<double>& t,
+                                         const DriftLayout& L, double* sw, int64_t ss,
+                                         const double* P, int64_t ps, int64_t out,
+                                         double* logj) {
+  const int ne = d.nelec, nmu = d.nmo_used, nc = 3 * ne;
+  const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
+  auto S = [&](int64_t item) -> double& { return sw[item * ss]; };
+  auto xyz = [&](int e, double (&p)[3]) {
+    for (int q = 0; q < 3; ++q) p[q] = P[(3 * e + q) * ps];
+  };
+  for (int e = 0; e < ne; ++e) {
+    const int64_t dst[4] = {L.ma + (int64_t)e * nmu, L.mx + (int64_t)e * nmu,
+                            L.my + (int64_t)e * nmu, L.mz + (int64_t)e * nmu};
+    drift_rows(t, nmu, sw, ss, L.ao, P[3 * e * ps], P[(3 * e + 1) * ps], P[(3 * e + 2) * ps],
+               dst);
+  }
+  for (int s = 0; s < 2; ++s)
+    for (int u = 0; u < d.ndet[s]; ++u) {
+      const int k = (s ? d.ndet[0] : 0) + u;
+      S(L.dv0 + k) = drift_det(d, L, sw, ss, s, u, -1, L.gd0 + (int64_t)k * nmax * 3);
+    }
+  const double wj = d.use_jastrow ? __ldg(d.jastrow_w) : 0.0;
+  double lj = 0.0;
+  for (int i = 0; i < ne; ++i) {
+    double g[3] = {0.0, 0.0, 0.0}, pi[3];
+    xyz(i, pi);
+    double ui = 0.0;
+    if (d.use_jastrow_en) {
+      const EnTerms en = en_terms(d, pi[0], pi[1], pi[2]);
+      lj += en.u;
+      for (int q = 0; q < 3; ++q) g[q] += en.g[q];
+    }
+    if (d.use_jastrow) {
+      for (int j = 0; j < ne; ++j) {
+        if (j == i) continue;
+        double pj[3], uj = 0.0;
+        xyz(j, pj);
+        pade_pair(same_spin(d, i, j) ? 0.25 : 0.5, wj, pi, pj, &uj, g);
+        if (j > i) ui += uj;
+      }
+    }
+    lj += ui;
+    for (int q = 0; q < 3; ++q) S(L.jg0 + 3 * i + q) = g[q];
+  }
+  const double sigma = drift_slater(d, L, sw, ss, -1, out);
+  for (int c = 0; c < nc; ++c) S(out + c) = S(out + c) / sigma + S(L.jg0 + c);
+  *logj = lj;
+  return sigma;
+}
+
 __global__ void __launch_bounds__(kDriftTPB) drift_kernel(const qmc_wf_desc d,
                                                           const qmc_drift_args a,
                                                           double* __restrict__ scr, int64_t ss,
@@ -154,70 +239,11 @@ __global__ void __launch_bounds__(kDriftTPB) drift_kernel(const qmc_wf_desc d,
     for (int q = 0; q < 3; ++q) p[q] = xs[3 * e + q];
   };
 
-  // ---- start positions: MO rows, spin determinants, Jastrow ----
-  for (int e = 0; e < ne; ++e) {
-    const int64_t dst[4] = {L.ma + (int64_t)e * nmu, L.mx + (int64_t)e * nmu,
-                            L.my + (int64_t)e * nmu, L.mz + (int64_t)e * nmu};
-    drift_rows(t, nmu, sw, ss, L.ao, xs[3 * e], xs[3 * e + 1], xs[3 * e + 2], dst);
-  }
   const int nmax = d.nup > d.ndown ? d.nup : d.ndown;
-  for (int s = 0; s < 2; ++s)
-    for (int u = 0; u < d.ndet[s]; ++u) {
-      const int k = (s ? d.ndet[0] : 0) + u;
-      S(L.dv0 + k) = drift_det(d, L, sw, ss, s, u, -1, L.gd0 + (int64_t)k * nmax * 3);
-    }
-  double logj0 = 0.0;
-  for (int i = 0; i < ne; ++i) {
-    double g[3] = {0.0, 0.0, 0.0}, pi[3];
-    xyz(i, pi);
-    double ui = 0.0;
-    if (d.use_jastrow_en) {
-      const EnTerms en = en_terms(d, pi[0], pi[1], pi[2]);
-      logj0 += en.u;
-      for (int q = 0; q < 3; ++q) g[q] += en.g[q];
-    }
-    if (d.use_jastrow) {
-      for (int j = 0; j < ne; ++j) {
-        if (j == i) continue;
-        double pj[3], uj = 0.0;
-        xyz(j, pj);
-        pade_pair(same_spin(d, i, j) ? 0.25 : 0.5, wj, pi, pj, &uj, g);
-        if (j > i) ui += uj;
-      }
-    }
-    logj0 += ui;
-    for (int q = 0; q < 3; ++q) S(L.jg0 + 3 * i + q) = g[q];
-  }
-
-  // psi and drift of a configuration: the moved spin sm's determinants from
-  // dvf / gdf (sm < 0: none moved), the others from dv0 / gd0; the Slater
-  // gradient sum goes to out[c], then out = grad Sigma / Sigma + grad log J
-  // (the Jastrow gradient added by the caller). Returns Sigma.
-  auto slater = [&](int sm, int64_t out) -> double {
-    for (int c = 0; c < nc; ++c) S(out + c) = 0.0;
-    double sigma = 0.0;
-    for (int k = 0; k < d.ncfg; ++k) {
-      const int uu = __ldg(d.cfg_det[0] + k), ud = __ldg(d.cfg_det[1] + k);
-      const int k0 = uu, k1 = d.ndet[0] + ud;
-      const double dv0 = S((sm == 0 ? L.dvf : L.dv0) + k0);
-      const double dv1 = S((sm == 1 ? L.dvf : L.dv0) + k1);
-      const double cd = __ldg(d.ci_weight + k) * dv0 * dv1;
-      sigma += cd;
-      for (int s = 0; s < 2; ++s) {
-        const int n = s ? d.ndown : d.nup, r0 = s ? d.nup : 0, kk = s ? k1 : k0;
-        const int64_t gd = (s == sm ? L.gdf : L.gd0) + (int64_t)kk * nmax * 3;
-        for (int i = 0; i < n; ++i)
-          for (int q = 0; q < 3; ++q)
-            S(out + 3 * (r0 + i) + q) = fma(cd, S(gd + i * 3 + q), S(out + 3 * (r0 + i) + q));
-      }
-    }
-    return sigma;
-  };
-
-  double rhoi;
+  // ---- start positions: MO rows, spin determinants, Jastrow, drift ----
+  double logj0, rhoi;
   {
-    const double sigma = slater(-1, L.dri);
-    for (int c = 0; c < nc; ++c) S(L.dri + c) = S(L.dri + c) / sigma + S(L.jg0 + c);
+    const double sigma = drift_full_eval(d, t, L, sw, ss, xs, 1, L.dri, &logj0);
     const double psi = exp(logj0) * sigma;
     rhoi = psi * psi;
     if (rhoi == 0.0) {
@@ -270,7 +296,7 @@ __global__ void __launch_bounds__(kDriftTPB) drift_kernel(const qmc_wf_desc d,
       const int k = (sm ? d.ndet[0] : 0) + u;
       S(L.dvf + k) = drift_det(d, L, sw, ss, sm, u, e, L.gdf + (int64_t)k * nmax * 3);
     }
-    const double sigma = slater(sm, L.drf);
+    const double sigma = drift_slater(d, L, sw, ss, sm, L.drf);
     // Jastrow: the pairs of e and its electron-nucleus terms change
     double logj = logj0, ge[3] = {0.0, 0.0, 0.0};
     if (d.use_jastrow_en) {
@@ -339,6 +365,98 @@ __global__ void __launch_bounds__(kDriftTPB) drift_kernel(const qmc_wf_desc d,
   if (a.accepted) a.accepted[w] += nacc;
 }
 
+// ---------------------------------------------------------------------------
+// Hamiltonian Monte Carlo (hamiltonian.py:75-201)
+// ---------------------------------------------------------------------------
+// Per step and walker: momenta p ~ N(0, I) over all 3 Ne coordinates,
+// H_start = U(q) + |p|^2 / 2 with U = -log psi^2, a leapfrog trajectory of L
+// steps of size eps (half momentum step, L - 1 full position + momentum steps,
+// a last position step and half momentum step) with the force
+// -grad U = 2 grad psi / psi from the full Jacobi evaluation at each point,
+// p negated, and the end point rejected when exp(H_start - H_end) < u. The
+// trajectory's positions, momenta and forces live in the walker's work
+// arrays (xi, dri, drf); pos holds the chain's current positions.
+__global__ void __launch_bounds__(kDriftTPB) hmc_kernel(const qmc_wf_desc d,
+                                                        const qmc_hmc_args a,
+                                                        double* __restrict__ scr, int64_t ss) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int ncol = round_up(d.nmo_used, 8);
+  const Tables<double> t = load_tables<double>(d, d.nmo_used, ncol, smem);
+  const int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= a.nwalkers) return;
+  const int nc = 3 * d.nelec;
+  const DriftLayout L = drift_layout(d);
+  double* sw = scr + w;
+  auto S = [&](int64_t item) -> double& { return sw[item * ss]; };
+  double* x0 = a.pos + w * nc;  // the chain's current positions
+  const double eps = a.step_size, heps = 0.5 * a.step_size;
+  const bool replay = a.momenta != nullptr;
+  Rng rng{(uint32_t)a.seed, (uint32_t)(a.seed >> 32), (uint32_t)w, 0, 0};
+  int nacc = 0, idecor = 0;
+  int64_t isnap = 0;
+  double* q = sw + L.xi * ss;  // trajectory positions, stride ss
+  for (int istep = 0; istep < a.nstep; ++istep) {
+    // momenta (replayed, or Box-Muller pairs of the step's Philox stream)
+    rng.step = a.step_offset + istep;
+    rng.call = 0;
+    double psq = 0.0;
+    for (int c = 0; c < nc; c += 4) {
+      double z[4];
+      if (replay) {
+        for (int k = 0; k < 4 && c + k < nc; ++k)
+          z[k] = a.momenta[((int64_t)istep * a.nwalkers + w) * nc + c + k];
+      } else {
+        const U4 r = rng.next();
+        rng.normal2(r.x, r.y, z[0], z[1]);
+        rng.normal2(r.z, r.w, z[2], z[3]);
+      }
+      for (int k = 0; k < 4 && c + k < nc; ++k) {
+        S(L.dri + c + k) = z[k];
+        psq = fma(z[k], z[k], psq);
+      }
+    }
+    for (int c = 0; c < nc; ++c) S(L.xi + c) = x0[c];
+    double logj;
+    double sigma = drift_full_eval(d, t, L, sw, ss, x0, 1, L.drf, &logj);
+    const double h0 = -2.0 * (logj + log(fabs(sigma))) + 0.5 * psq;
+    // half step in momentum: p -= (eps / 2) grad U, grad U = -2 grad log psi
+    for (int c = 0; c < nc; ++c)
+      S(L.dri + c) = __dsub_rn(S(L.dri + c), __dmul_rn(heps, -2.0 * S(L.drf + c)));
+    for (int l = 0; l < a.traj_length; ++l) {
+      for (int c = 0; c < nc; ++c) q[c * ss] = __dadd_rn(q[c * ss], __dmul_rn(eps, S(L.dri + c)));
+      sigma = drift_full_eval(d, t, L, sw, ss, q, ss, L.drf, &logj);
+      const double f = l + 1 < a.traj_length ? eps : heps;  // the last momentum step is a half step
+      for (int c = 0; c < nc; ++c)
+        S(L.dri + c) = __dsub_rn(S(L.dri + c), __dmul_rn(f, -2.0 * S(L.drf + c)));
+    }
+    // p is negated before the kinetic energy, which its sign does not change
+    psq = 0.0;
+    for (int c = 0; c < nc; ++c) psq = fma(S(L.dri + c), S(L.dri + c), psq);
+    const double h1 = -2.0 * (logj + log(fabs(sigma))) + 0.5 * psq;
+    double u;
+    if (replay) {
+      u = a.uniforms[(int64_t)istep * a.nwalkers + w];
+    } else {
+      rng.call = (uint32_t)((nc + 3) / 4);
+      const U4 r = rng.next();
+      u = rng.uniform53(r.x, r.y);
+    }
+    if (!(exp(h0 - h1) < u)) {
+      ++nacc;
+      for (int c = 0; c < nc; ++c) x0[c] = q[c * ss];
+    }
+    if (istep >= a.ntherm) {
+      if (idecor % a.ndecor == 0 && a.samples && isnap < a.nsnap) {
+        double* o = a.samples + (isnap * a.nwalkers + w) * nc;
+        for (int c = 0; c < nc; ++c) o[c] = x0[c];
+        ++isnap;
+      }
+      ++idecor;
+    }
+  }
+  if (a.accepted) a.accepted[w] += nacc;
+}
+
 }  // namespace qmc
 
 using namespace qmc;
@@ -375,6 +493,35 @@ int qmc_drift_run(const qmc_wf_desc* d0, const qmc_drift_args* a, void* scratch,
   const double sd = sqrt(sqrt(a->step_size));  // covariance sqrt(step) I
   drift_kernel<<<grid, kDriftTPB, smem, (cudaStream_t)stream>>>(
       dd, *a, (double*)scratch, pad_walkers(a->nwalkers), sd);
+  return launch_status();
+}
+
+int64_t qmc_hmc_scratch_bytes(const qmc_wf_desc* d, int64_t nw) {
+  return qmc_drift_scratch_bytes(d, nw);
+}
+
+int qmc_hmc_run(const qmc_wf_desc* d0, const qmc_hmc_args* a, void* scratch,
+                int64_t scratch_bytes, void* stream) {
+  int st = check_desc(d0);
+  if (st) return st;
+  if (!a) return QMC_ERR_ARG;
+  qmc_wf_desc dd = *d0;
+  dd.precision = QMC_PREC_FP64;  // the HMC sampler is FP64
+  const qmc_wf_desc* d = &dd;
+  if (a->nwalkers < 0 || a->nstep < 0 || a->ntherm < 0 || a->ndecor < 1 || a->nsnap < 0 ||
+      a->traj_length < 1 || !(a->step_size > 0.0))
+    return QMC_ERR_ARG;
+  if ((a->momenta != nullptr) != (a->uniforms != nullptr)) return QMC_ERR_ARG;
+  if (a->nwalkers == 0 || a->nstep == 0) return QMC_OK;
+  if (!a->pos || !scratch) return QMC_ERR_ARG;
+  if (a->nsnap > 0 && !a->samples) return QMC_ERR_ARG;
+  if (scratch_bytes < qmc_hmc_scratch_bytes(d, a->nwalkers)) return QMC_ERR_SCRATCH;
+  const int ncol = round_up(d->nmo_used, 8);
+  const int64_t smem = tables_smem_bytes<double>(*d, ncol);
+  if ((st = prepare_smem(hmc_kernel, smem))) return st;
+  const dim3 grid((unsigned)((a->nwalkers + kDriftTPB - 1) / kDriftTPB));
+  hmc_kernel<<<grid, kDriftTPB, smem, (cudaStream_t)stream>>>(dd, *a, (double*)scratch,
+                                                               pad_walkers(a->nwalkers));
   return launch_status();
 }
 

@@ -12,12 +12,16 @@ keep to reproduce its chains:
 * the kept positions are those after each step, from ``ntherm`` on, every
   ``ndecor`` steps (hamiltonian.py:113-131).
 
-When ``pdf`` is the bound ``pdf`` of a wave function of this package, the
-force -grad U = grad(pdf) / pdf comes from its Jacobi gradient kernel
-(``pdf(x, return_grad=True)``, ``qmc_wf_gradients``) and one density call
-(``qmc_wf_psi``), instead of autograd through the density; any other callable
-is differentiated with autograd as in the reference (get_grad, 40-61). The
-trajectory runs on the host: two kernel calls per leapfrog step.
+When ``pdf`` is the bound ``pdf`` of a wave function of this package (and
+``ndim`` is 3), the whole call is one ``qmc_hmc_run`` launch: every walker's
+trajectories run on the device, the force -grad U = 2 grad psi / psi from the
+Jacobi formula at each leapfrog point. Its random numbers come from the device
+generator (Philox, keyed by ``seed`` or by a draw from torch's generator) with
+``rng="device"``, the default; with ``rng="torch"`` they are drawn from torch's
+CPU generator in the reference's order (momenta, then acceptance uniforms, per
+step) and handed to the kernel, so that with the same torch seed the chains are
+the reference's. Any other callable runs the host loop, differentiated with
+autograd as in the reference (get_grad, 40-61).
 """
 from __future__ import annotations
 
@@ -25,6 +29,9 @@ import logging
 
 import torch
 
+from .. import _lib
+from ..wavefunction import runtime as rt
+from .generalized_metropolis import GeneralizedMetropolis
 from .metropolis import SamplerBase
 
 log = logging.getLogger("qmctorch_gb300")
@@ -34,10 +41,71 @@ class Hamiltonian(SamplerBase):
     """hamiltonian.py:10-38 (same arguments and defaults)."""
 
     def __init__(self, nwalkers=100, nstep=100, step_size=0.2, L=10, ntherm=-1, ndecor=1,
-                 nelec=1, ndim=3, init={"min": -5, "max": 5}, cuda=False):  # noqa: B006
+                 nelec=1, ndim=3, init={"min": -5, "max": 5}, cuda=False,  # noqa: B006
+                 rng="device", seed=None):
         SamplerBase.__init__(self, nwalkers, nstep, step_size, ntherm, ndecor, nelec, ndim,
                              init, cuda)
         self.traj_length = L
+        if rng not in ("device", "torch"):
+            raise ValueError("rng should be 'device' or 'torch'")
+        self.rng = rng
+        self._seed = None if seed is None else int(seed)
+        self._step_counter = 0
+        self.last_acceptance = None
+
+    seed = GeneralizedMetropolis.seed
+
+    def reference_draws(self, nwalkers):
+        """The random numbers of one call in the reference's order, from
+        torch's default CPU generator: per step the momenta (``_step``'s
+        ``torch.randn``) and the acceptance uniforms (``torch.rand``).
+        Returns (momenta [nstep, nw, nelec * ndim], uniforms [nstep, nw]), FP64."""
+        nc = self.nelec * self.ndim
+        mom = torch.empty((self.nstep, nwalkers, nc), dtype=torch.float64)
+        unif = torch.empty((self.nstep, nwalkers), dtype=torch.float64)
+        for istep in range(self.nstep):
+            mom[istep] = torch.randn((nwalkers, nc)).double()
+            unif[istep] = torch.rand(nwalkers).double()
+        return mom, unif
+
+    def _run_kernel(self, wf):
+        """One ``qmc_hmc_run`` launch for the whole call."""
+        nsnap = len(range(self.ntherm, self.nstep, self.ndecor))
+        if nsnap == 0:
+            raise RuntimeError("no samples kept: ntherm >= nstep")
+        device = rt.cuda_device()
+        src = self.walkers.pos.detach()
+        x = rt.dev64(src, device)
+        if x.data_ptr() == src.data_ptr():
+            x = x.clone()
+        nw = x.shape[0]
+        nc = self.nelec * self.ndim
+        samples = torch.empty((nsnap, nw, nc), dtype=rt.F64, device=device)
+        acc = torch.zeros(nw, dtype=torch.int32, device=device)
+        call = wf._desc(device)
+        lib = _lib.lib()
+        scr = rt.scratch(lib.qmc_hmc_scratch_bytes(call.ref, nw), device)
+        a = _lib.HmcArgs()
+        a.pos, a.nwalkers, a.nstep = rt.ptr(x), nw, self.nstep
+        a.ntherm, a.ndecor, a.traj_length = self.ntherm, self.ndecor, int(self.traj_length)
+        a.step_size = float(self.step_size)
+        a.samples, a.nsnap, a.accepted = rt.ptr(samples), nsnap, rt.ptr(acc)
+        keep = []
+        if self.rng == "torch":
+            mom, unif = self.reference_draws(nw)
+            keep = [mom.to(device), unif.to(device)]
+            a.momenta, a.uniforms = rt.ptr(keep[0]), rt.ptr(keep[1])
+        else:
+            a.seed, a.step_offset = self.seed, self._step_counter
+        _lib.check(lib.qmc_hmc_run(call.ref, a, rt.ptr(scr), scr.numel(), rt.stream_handle()),
+                   "qmc_hmc_run")
+        self._step_counter += self.nstep
+        self.last_acceptance = float(acc.sum()) / max(1, nw * self.nstep)
+        log.debug("  Acceptance rate %1.3f %%", self.last_acceptance * 100)
+        self.walkers.pos = x.to(device=src.device, dtype=src.dtype)
+        del keep
+        return samples.reshape(nsnap * nw, nc).to(device=src.device,
+                                                  dtype=src.dtype).requires_grad_()
 
     @staticmethod
     def get_grad(func, inp):
@@ -76,6 +144,10 @@ class Hamiltonian(SamplerBase):
             self.ntherm = self.nstep + self.ntherm
         self.walkers.initialize(pos=pos)
         self.walkers.pos = self.walkers.pos.clone()
+        wf = GeneralizedMetropolis._wavefunction(pdf)
+        if wf is not None and self.ndim == 3:
+            with torch.no_grad():
+                return self._run_kernel(wf)
         owner = getattr(pdf, "__self__", None)
         if owner is not None and hasattr(owner, "gradients_jacobi"):
             potential, grad = self._kernel_potential(pdf)
@@ -90,7 +162,8 @@ class Hamiltonian(SamplerBase):
                 if idecor % self.ndecor == 0:
                     kept.append(self.walkers.pos)
                 idecor += 1
-        log.debug("  Acceptance rate %1.3f %%", rate / max(self.nstep, 1) * 100)
+        self.last_acceptance = rate / max(self.nstep, 1)
+        log.debug("  Acceptance rate %1.3f %%", self.last_acceptance * 100)
         return torch.cat(kept).requires_grad_()
 
     @staticmethod

@@ -1,14 +1,27 @@
-"""HMC on an H2 sto-3g SlaterJastrow of this package, forces from the Jacobi
-gradient kernel (qmc_wf_gradients) and densities from the psi kernel, against
-the reference sampler's chains on its own H2 wave function with autograd
-forces (tests/golden/hamiltonian.npz), same seed and initial walkers. The
-forces agree to rounding (the Jacobi gradient equals the autograd gradient to
-~1e-15), so 12 steps of 6 leapfrog steps stay within 1e-9."""
+"""GPU tests of the HMC sampler on wave functions of this package (one
+qmc_hmc_run launch per call).
+
+* With ``rng="torch"`` the kernel consumes the reference's random draws, so
+  its chains are compared with the chains of the reference's Hamiltonian on
+  its own H2 sto-3g SlaterJastrow with autograd forces
+  (tests/golden/hamiltonian.npz), same seed and initial walkers: the forces
+  agree to rounding (the Jacobi gradient equals the autograd gradient to
+  ~1e-15), so 12 steps of 6 leapfrog steps stay within 1e-9.
+* On H2O cc-pVDZ single_double(4,4) and LiH with the combined e-e and e-n
+  Jastrow the kernel is compared with this package's host loop (density by
+  qmc_wf_psi, force by qmc_wf_gradients) on the same draws: 1e-9.
+* With the device generator the chains are reproducible and accept at the
+  rate of the torch-drawn chains. (A trajectory whose end energy is NaN is
+  accepted, as the reference's `exp(H0 - H1) < u` rejection test implies.)
+"""
+import os
+
 import numpy as np
 import pytest
 import torch
 
 from tests.golden_cases import GOLDEN, load
+from tests.golden_cases import make_wf as golden_make_wf
 
 pytestmark = pytest.mark.gpu
 
@@ -16,9 +29,19 @@ HMC = {"nwalkers": 16, "nelec": 2, "ndim": 3, "nstep": 12, "step_size": 0.1, "L"
        "ntherm": -6, "ndecor": 2, "seed": 777}
 
 
-def test_hmc_chains_match_reference_on_h2():
-    import os
+class HostLoopPdf:
+    """wf.pdf under another name: the sampler runs its host loop, with the
+    force from the wave function's Jacobi gradient kernel."""
 
+    def __init__(self, wf):
+        self.__self__ = wf
+        self.__name__ = "pdf_host_loop"
+
+    def __call__(self, x, return_grad=False):
+        return self.__self__.pdf(x, return_grad=return_grad)
+
+
+def test_hmc_chains_match_reference_on_h2():
     from qmctorch_gb300.sampler import Hamiltonian
     from qmctorch_gb300.wavefunction import SlaterJastrow
     torch.set_default_dtype(torch.float64)
@@ -29,8 +52,64 @@ def test_hmc_chains_match_reference_on_h2():
     g = HMC
     s = Hamiltonian(nwalkers=g["nwalkers"], nstep=g["nstep"], step_size=g["step_size"], L=g["L"],
                     ntherm=g["ntherm"], ndecor=g["ndecor"], nelec=g["nelec"], ndim=g["ndim"],
-                    init={"method": "uniform", "min": -1, "max": 1}, cuda=True)
+                    init={"method": "uniform", "min": -1, "max": 1}, cuda=True, rng="torch")
     torch.manual_seed(g["seed"] + 1)
     out = s(wf.pdf, pos=torch.as_tensor(gold["h2_pos0"], device="cuda"), with_tqdm=False)
     np.testing.assert_allclose(out.detach().cpu().numpy(), gold["h2_samples"], rtol=1e-9,
                                atol=1e-9)
+
+
+def start_positions(d, nw, seed):
+    rng = np.random.default_rng(seed)
+    return torch.as_tensor(np.repeat(d["pos"], -(-nw // len(d["pos"])), axis=0)[:nw]
+                           + 0.05 * rng.standard_normal((nw, d["pos"].shape[1])), device="cuda")
+
+
+@pytest.mark.parametrize("name", ["h2o_sd", "lih_en"])
+def test_hmc_kernel_matches_the_host_loop(name):
+    from qmctorch_gb300.sampler import Hamiltonian
+    mol, d = load(name)
+    wf = golden_make_wf(mol, d)
+    nw = 256
+    pos0 = start_positions(d, nw, 7)
+    runs = []
+    for pdf in (wf.pdf, HostLoopPdf(wf)):
+        s = Hamiltonian(nwalkers=nw, nstep=10, step_size=0.02, L=5, ntherm=-5, ndecor=2,
+                        nelec=mol.nelec, ndim=3, cuda=True, rng="torch")
+        torch.manual_seed(4321)
+        out = s(pdf, pos=pos0.clone(), with_tqdm=False)
+        runs.append((out.detach().cpu().numpy(), s.walkers.pos.detach().cpu().numpy(),
+                     s.last_acceptance))
+    (ko, kf, ka), (ho, hf, ha) = runs
+    assert ko.shape == ho.shape == (3 * nw, 3 * mol.nelec)
+    assert 0.1 < ka < 1.0 and abs(ka - ha) < 1e-12
+    np.testing.assert_allclose(ko, ho, rtol=0, atol=1e-9)
+    np.testing.assert_allclose(kf, hf, rtol=0, atol=1e-9)
+
+
+def test_hmc_device_generator_chains():
+    from qmctorch_gb300.sampler import Hamiltonian
+    mol, d = load("h2o_sd")
+    wf = golden_make_wf(mol, d)
+    nw = 2048
+    pos0 = start_positions(d, nw, 11)
+
+    def run(kind, seed):
+        s = Hamiltonian(nwalkers=nw, nstep=8, step_size=0.02, L=5, ntherm=0, ndecor=1,
+                        nelec=mol.nelec, ndim=3, cuda=True, rng=kind, seed=seed)
+        torch.manual_seed(99)
+        out = s(wf.pdf, pos=pos0.clone(), with_tqdm=False)
+        return out.detach().cpu().numpy(), s.last_acceptance
+
+    a, acc_a = run("device", 5)
+    b, acc_b = run("device", 5)
+    c, acc_c = run("device", 6)
+    t, acc_t = run("torch", None)
+    # a trajectory whose end energy is NaN (a force overflow near a node) is
+    # accepted, as the reference's `exp(H0 - H1) < u` test does: compare NaN
+    # positions as equal
+    assert np.array_equal(a, b, equal_nan=True) and acc_a == acc_b, \
+        int((~np.isclose(a, b, rtol=0, atol=0, equal_nan=True)).sum())
+    assert not np.array_equal(a, c, equal_nan=True)
+    assert 0.1 < acc_t < 1.0
+    assert abs(acc_a - acc_t) < 0.03 and abs(acc_c - acc_t) < 0.03

@@ -300,3 +300,29 @@ def test_drift_sampler_rejects_bad_arguments_without_a_gpu(name):
     assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
     a.nsnap, a.nstep = 0, 0
     assert lib.qmc_drift_run(ctypes.byref(desc), ctypes.byref(a), None, 0, None) == 0
+
+
+def test_hmc_sampler_rejects_bad_arguments_without_a_gpu():
+    """qmc_hmc_run checks its arguments (step, trajectory length, decorrelation,
+    replay inputs both or none, snapshot buffer, scratch size) before any
+    device call; an empty run is a no-op."""
+    lib = _lib.lib()
+    desc, keep, wf = _desc_for("h2o_sd")
+    v = ctypes.c_void_p(8)
+    a = _lib.HmcArgs()
+    a.pos, a.nwalkers, a.nstep, a.ntherm, a.ndecor = v, 16, 4, 0, 1
+    a.traj_length, a.step_size = 5, 0.1
+    need = lib.qmc_hmc_scratch_bytes(ctypes.byref(desc), 16)
+    assert need > 0
+    assert lib.qmc_hmc_run(ctypes.byref(desc), None, v, need, None) == 1
+    assert lib.qmc_hmc_run(ctypes.byref(desc), ctypes.byref(a), v, need - 8, None) == 3
+    a.traj_length = 0
+    assert lib.qmc_hmc_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.traj_length, a.step_size = 5, -0.1
+    assert lib.qmc_hmc_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.step_size, a.momenta = 0.1, v  # replay needs both inputs
+    assert lib.qmc_hmc_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.momenta, a.nsnap = None, 3  # snapshots without a buffer
+    assert lib.qmc_hmc_run(ctypes.byref(desc), ctypes.byref(a), v, need, None) == 1
+    a.nsnap, a.nstep = 0, 0
+    assert lib.qmc_hmc_run(ctypes.byref(desc), ctypes.byref(a), None, 0, None) == 0
