@@ -466,14 +466,14 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
       for (int j = KIN ? 0 : e + 1; j < ne; ++j) {
         if (j == e) continue;
         const R dx = dif(ex, pw[3 * j]), dy = dif(ey, pw[3 * j + 1]), dz = dif(ez, pw[3 * j + 2]);
-        const R r = rsqrt_(dx * dx + dy * dy + dz * dz);
-        if (KIN) vs += (R)1 / r;
+        const R r = psqrt(dx * dx + dy * dy + dz * dz);
+        if (KIN) vs += prcp(r);
         if (d.use_jastrow) {
           const R w0 = same_spin(d, e, j) ? (R)0.25 : (R)0.5;
-          const R iu = (R)1 / ((R)1 + w * r);
+          const R iu = prcp((R)1 + w * r);
           ks += w0 * r * iu;
           if (KIN) {
-            const R ir = (R)1 / r;
+            const R ir = prcp(r);
             const R k1 = w0 * iu * iu;                       // dK/dr
             gx += k1 * dx * ir;
             gy += k1 * dy * ir;
@@ -490,11 +490,11 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
       for (int A = 0; A < t.natom; ++A) {
         const R dx = dif(ex, t.en_p[3 * A]), dy = dif(ey, t.en_p[3 * A + 1]),
                 dz = dif(ez, t.en_p[3 * A + 2]);
-        const R r = rsqrt_(dx * dx + dy * dy + dz * dz);
-        const R iu = (R)1 / ((R)1 + wn * r);
+        const R r = psqrt(dx * dx + dy * dy + dz * dz);
+        const R iu = prcp((R)1 + wn * r);
         kn += r * iu;
         if (KIN) {
-          const R ir = (R)1 / r;
+          const R ir = prcp(r);
           const R k1 = iu * iu;  // dK/dr
           gx += k1 * dx * ir;
           gy += k1 * dy * ir;
@@ -510,7 +510,7 @@ __device__ inline void ep_electron(const qmc_wf_desc& d, const Tables<R>& t, con
       for (int A = 0; A < t.natom; ++A) {
         const R dx = dif(ex, t.atom_p[3 * A]), dy = dif(ey, t.atom_p[3 * A + 1]),
                 dz = dif(ez, t.atom_p[3 * A + 2]);
-        ven -= (R)t.atom_z[A] / rsqrt_(dx * dx + dy * dy + dz * dz);
+        ven -= pdiv((R)t.atom_z[A], psqrt(dx * dx + dy * dy + dz * dz));
       }
       *vrow = 0.5 * (double)vs + (double)ven;
     } else {
